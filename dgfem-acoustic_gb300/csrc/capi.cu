@@ -1,0 +1,824 @@
+// C ABI of the GB300 DG solver (include/dgfem_gb300.h): context lifetime,
+// state I/O in the reference layout, sources, observers, the per-step CUDA
+// graph (source injection -> four fused RK4 stages -> residual and observer
+// reductions) and benchmarking.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------
+// auxiliary kernels
+// ---------------------------------------------------------------------------
+
+// reference layout [4][E*np] (double, mesh local node order) -> internal
+template <typename T>
+__global__ void k_ref_to_int(const double* ref, T* out, const int* perm, int64_t E, int np, int nv, int64_t stride) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nv * E * np) return;
+  int q = (int)(i / (E * np));
+  int64_t r = i - (int64_t)q * E * np;
+  int64_t e = r / np;
+  int n = (int)(r - e * np);
+  out[q * stride + e * np + perm[n]] = (T)ref[i];
+}
+
+template <typename T>
+__global__ void k_int_to_ref(const T* in, double* ref, const int* perm, int64_t E, int np, int nv, int64_t stride) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 4 * E * np) return;
+  int q = (int)(i / (E * np));
+  int64_t r = i - (int64_t)q * E * np;
+  int64_t e = r / np;
+  int n = (int)(r - e * np);
+  ref[i] = q < nv ? (double)in[q * stride + e * np + perm[n]] : 0.0;
+}
+
+// Hard overwrite of the pressure at source nodes (src/solver.cpp:455-483):
+// per node, the last source (in order) that is active at this step wins.
+template <typename T>
+__global__ void k_inject(T* up, const int64_t* dof, const int* off, const int* ids, const double* val, int nsrc,
+                         int64_t nrows, const int64_t* step, int64_t ndof) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= ndof) return;
+  int64_t s = step[0];
+  if (s < 0 || s >= nrows) return;
+  const double* row = val + s * nsrc;
+  double v = 0.0;
+  bool any = false;
+  for (int k = off[i]; k < off[i + 1]; ++k) {
+    double x = row[ids[k]];
+    if (!isnan(x)) v = x, any = true;
+  }
+  if (any) up[dof[i]] = (T)v;
+}
+
+// Residuals (block 0) and observer IDW samples (blocks 1..n_obs) of the step
+// just completed (src/solver.cpp:518-573).
+template <typename T>
+__global__ void k_finalize(const double* partials, int nparts, double inv_count, double* res, const T* u,
+                           int64_t stride, int nv, const int64_t* odof, const int64_t* ooff, const double* ow,
+                           double* obs, int n_obs, const int64_t* step, int64_t cap) {
+  __shared__ double sh[32][5];
+  int64_t slot = step[0] - step[1];
+  if (slot < 0 || slot >= cap) return;
+  const int tid = threadIdx.x;
+  if (blockIdx.x == 0) {
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int b = tid; b < nparts; b += blockDim.x)
+      for (int c = 0; c < 5; ++c) acc[c] += partials[b * 5 + c];
+    for (int c = 0; c < 5; ++c) {
+      double v = acc[c];
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if ((tid & 31) == 0) sh[tid >> 5][c] = v;
+    }
+    __syncthreads();
+    if (tid < 5) {
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w][tid];
+      res[slot * 5 + tid] = v * inv_count;
+    }
+    return;
+  }
+  int o = blockIdx.x - 1;
+  if (o >= n_obs) return;
+  double acc[5] = {0, 0, 0, 0, 0};  // p, vx, vy, vz, w
+  for (int64_t k = ooff[o] + tid; k < ooff[o + 1]; k += blockDim.x) {
+    double w = ow[k];
+    int64_t d = odof[k];
+    for (int q = 0; q < nv; ++q) acc[q] += (double)u[q * stride + d] * w;
+    acc[4] += w;
+  }
+  for (int c = 0; c < 5; ++c) {
+    double v = acc[c];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((tid & 31) == 0) sh[tid >> 5][c] = v;
+  }
+  __syncthreads();
+  if (tid < 4) {
+    double v = 0.0, w = 0.0;
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) v += sh[ww][tid], w += sh[ww][4];
+    obs[(slot * n_obs + o) * 4 + tid] = v / w;
+  }
+}
+
+__global__ void k_advance(int64_t* step) { step[0] += 1; }
+
+// Euler1 commit: u = y (computed as u + k by the stage kernel) with residuals.
+template <typename T>
+__global__ void k_euler_commit(T* u, const T* y, const T* snap, int64_t n, int64_t stride, int nv, double c0sq,
+                               double* partials) {
+  __shared__ double sh[32][5];
+  double red[5] = {0, 0, 0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int q = (int)(i / stride);
+    T un = y[i];
+    u[i] = un;
+    double dn = (double)snap[i] - (double)un;
+    if (q == 0) {
+      red[0] += dn * dn;
+      double dr = (double)snap[i] / c0sq - (double)un / c0sq;
+      red[1] += dr * dr;
+    } else {
+      red[1 + q] += dn * dn;
+    }
+  }
+  const int tid = threadIdx.x;
+  for (int c = 0; c < 5; ++c) {
+    double v = red[c];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((tid & 31) == 0) sh[tid >> 5][c] = v;
+  }
+  __syncthreads();
+  if (tid < 5) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w][tid];
+    partials[blockIdx.x * 5 + tid] = v;
+  }
+}
+
+// Element means of p, p/c0^2 and v (src/Mesh.cpp:1196-1212), mesh node order.
+template <typename T>
+__global__ void k_cell_means(const T* u, const int* perm, int64_t E, int np, int nv, int64_t stride, double c0sq,
+                             double* out) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double p = 0, rho = 0, v[3] = {0, 0, 0};
+  for (int n = 0; n < np; ++n) {
+    int64_t g = e * np + perm[n];
+    double pv = (double)u[g];
+    p += pv;
+    rho += pv / c0sq;
+    for (int d = 0; d < nv - 1; ++d) v[d] += (double)u[(1 + d) * stride + g];
+  }
+  out[e * 5 + 0] = p / np;
+  out[e * 5 + 1] = rho / np;
+  for (int d = 0; d < 3; ++d) out[e * 5 + 2 + d] = v[d] / np;
+}
+
+__global__ void k_flush(unsigned* buf, int64_t n, unsigned v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    buf[i] = v + (unsigned)i;
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+int fail(dg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(c, x)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (x);                                                                      \
+    if (e_ != cudaSuccess) return fail((c), DG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_out, double dt) {
+  dgk::StageArgs<T> a{};
+  a.y_in = y_in;
+  a.y_out = y_out;
+  a.u = (T*)c->u;
+  a.acc = (T*)c->acc;
+  a.snap = (const T*)c->snap;
+  a.k_out = k_out;
+  a.partials = c->partials;
+  a.geoF = (const T*)c->geoF;
+  a.geoI = c->geoI;
+  a.bmat = (const T*)c->bmat;
+  a.Dt = (const T*)c->Dt;
+  a.LIFT = (const T*)c->LIFT;
+  a.fmask = c->fmask;
+  a.nbrnode = c->nbrnode;
+  a.stride = c->Epad * c->np;
+  a.ntiles = (int)c->ntiles;
+  a.stage = stage;
+  a.dt = dt;
+  a.c0sq = c->c0sq;
+  a.ph = c->ph;
+  if constexpr (sizeof(T) == 4)
+    return c->dim == 2 ? dgk::launch_stage_f32_2d(c->order, a, c->grid, c->stream)
+                       : dgk::launch_stage_f32_3d(c->order, a, c->grid, c->stream);
+  else
+    return c->dim == 2 ? dgk::launch_stage_f64_2d(c->order, a, c->grid, c->stream)
+                       : dgk::launch_stage_f64_3d(c->order, a, c->grid, c->stream);
+}
+
+cudaError_t launch_stage(dg_ctx* c, int stage, const void* y_in, void* y_out, void* k_out, double dt) {
+  if (c->prec == DG_FP32) return launch_stage_t<float>(c, stage, (const float*)y_in, (float*)y_out, (float*)k_out, dt);
+  return launch_stage_t<double>(c, stage, (const double*)y_in, (double*)y_out, (double*)k_out, dt);
+}
+
+// One time step on c->stream. kind 0: RK4, 1: Euler1. ev (optional, 8
+// events) brackets the stage launches for kernel timing.
+cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
+  cudaError_t err;
+  const int64_t stride = c->Epad * c->np;
+  if (c->n_src_dofs > 0) {
+    if (c->prec == DG_FP32)
+      k_inject<float><<<nblk(c->n_src_dofs, 128), 128, 0, c->stream>>>(
+          (float*)c->u, c->d_src_dof, c->d_src_off, c->d_src_ids, c->d_srcval, c->n_src, c->srcval_steps, c->d_step,
+          c->n_src_dofs);
+    else
+      k_inject<double><<<nblk(c->n_src_dofs, 128), 128, 0, c->stream>>>(
+          (double*)c->u, c->d_src_dof, c->d_src_off, c->d_src_ids, c->d_srcval, c->n_src, c->srcval_steps, c->d_step,
+          c->n_src_dofs);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  int nparts = c->grid;
+  if (kind == 0) {
+    const void* in[4] = {c->u, c->y0, c->y1, c->y0};
+    void* out[4] = {c->y0, c->y1, c->y0, nullptr};
+    for (int s = 0; s < 4; ++s) {
+      if (ev) cudaEventRecord(ev[2 * s], c->stream);
+      if ((err = launch_stage(c, s + 1, in[s], out[s], nullptr, dt)) != cudaSuccess) return err;
+      if (ev) cudaEventRecord(ev[2 * s + 1], c->stream);
+    }
+  } else {
+    if (ev) cudaEventRecord(ev[0], c->stream);
+    if ((err = launch_stage(c, 5, c->u, c->y0, nullptr, dt)) != cudaSuccess) return err;
+    if (ev) cudaEventRecord(ev[1], c->stream);
+    const int cb = 2 * c->num_sms;
+    nparts = cb;
+    int64_t n = (int64_t)c->nv * stride;
+    if (c->prec == DG_FP32)
+      k_euler_commit<float><<<cb, 256, 0, c->stream>>>((float*)c->u, (const float*)c->y0, (const float*)c->snap, n,
+                                                       stride, c->nv, c->c0sq, c->partials);
+    else
+      k_euler_commit<double><<<cb, 256, 0, c->stream>>>((double*)c->u, (const double*)c->y0, (const double*)c->snap,
+                                                        n, stride, c->nv, c->c0sq, c->partials);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  double inv_count = 1.0 / (double)(c->E * c->np);
+  if (c->prec == DG_FP32)
+    k_finalize<float><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res, (const float*)c->u,
+                                                          stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w,
+                                                          c->d_obs, c->n_obs, c->d_step, c->out_cap);
+  else
+    k_finalize<double><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res,
+                                                           (const double*)c->u, stride, c->nv, c->d_obs_dof,
+                                                           c->d_obs_off, c->d_obs_w, c->d_obs, c->n_obs, c->d_step,
+                                                           c->out_cap);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  k_advance<<<1, 1, 0, c->stream>>>(c->d_step);
+  return cudaGetLastError();
+}
+
+int ensure_out_cap(dg_ctx* c, int64_t n) {
+  if (n <= c->out_cap) return DG_OK;
+  int64_t cap = std::max<int64_t>(n, 1024);
+  if (c->d_res) cudaFree(c->d_res);
+  if (c->d_obs) cudaFree(c->d_obs);
+  c->d_res = nullptr, c->d_obs = nullptr;
+  CK(c, cudaMalloc(&c->d_res, cap * 5 * sizeof(double)));
+  CK(c, cudaMalloc(&c->d_obs, cap * std::max(1, c->n_obs) * 4 * sizeof(double)));
+  c->out_cap = cap;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  return DG_OK;
+}
+
+int build_graph(dg_ctx* c, int kind, double dt) {
+  if (c->graph && c->graph_dt == dt && c->graph_kind == kind) return DG_OK;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = enqueue_step(c, kind, dt, nullptr);
+  cudaError_t err2 = cudaStreamEndCapture(c->stream, &g);
+  if (err != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("CUDA (capture): ") + cudaGetErrorString(err));
+  CK(c, err2);
+  err = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(c, err);
+  c->graph_dt = dt;
+  c->graph_kind = kind;
+  return DG_OK;
+}
+
+int run_steps(dg_ctx* c, int kind, int64_t n_steps, double dt, double* residuals, double* obs) {
+  if (!c) return DG_ERR_ARG;
+  if (n_steps < 0 || !(dt > 0)) return fail(c, DG_ERR_ARG, "n_steps must be >= 0 and dt > 0");
+  if (n_steps == 0) return DG_OK;
+  int rc = ensure_out_cap(c, n_steps);
+  if (rc) return rc;
+  rc = build_graph(c, kind, dt);
+  if (rc) return rc;
+  int64_t st[2] = {c->step, c->step};
+  CK(c, cudaMemcpyAsync(c->d_step, st, sizeof(st), cudaMemcpyHostToDevice, c->stream));
+  for (int64_t i = 0; i < n_steps; ++i) CK(c, cudaGraphLaunch(c->graph, c->stream));
+  std::vector<double> res(n_steps * 5);
+  CK(c, cudaMemcpyAsync(res.data(), c->d_res, n_steps * 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (obs && c->n_obs > 0)
+    CK(c, cudaMemcpyAsync(obs, c->d_obs, n_steps * c->n_obs * 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->step += n_steps;
+  if (residuals) std::memcpy(residuals, res.data(), res.size() * sizeof(double));
+  for (double v : res)
+    if (!std::isfinite(v)) return fail(c, DG_ERR_NONFINITE, "non-finite values in the state (residual is NaN/Inf)");
+  return DG_OK;
+}
+
+template <typename T>
+void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>& L) {
+  const int np = re.np, D = re.dim, nk = re.nf * re.nfp;
+  Dt.resize(D * np * np);
+  for (int r = 0; r < D; ++r)
+    for (int j = 0; j < np; ++j)
+      for (int i = 0; i < np; ++i) Dt[(r * np + j) * np + i] = (T)re.Dt[(r * np + i) * np + j];
+  L.resize(nk * np);
+  for (int k = 0; k < nk; ++k)
+    for (int i = 0; i < np; ++i) L[k * np + i] = (T)re.LIFT[i * nk + k];
+}
+
+}  // namespace
+
+namespace dgc {
+cudaError_t dev_alloc(dg_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes + 64);
+  if (e == cudaSuccess) {
+    c->allocs.push_back(*p);
+    c->device_bytes += (int64_t)bytes;
+  }
+  return e;
+}
+}  // namespace dgc
+
+extern "C" {
+
+const char* dg_last_error(const dg_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out) {
+  if (!out) return DG_ERR_ARG;
+  *out = nullptr;
+  auto bad = [&](int code, const std::string& m) {
+    g_create_error = m;
+    return code;
+  };
+  if (!mesh || !phys || !mesh->xyz || !mesh->elem_nodes) return bad(DG_ERR_ARG, "null mesh or physics");
+  if (mesh->dim != 2 && mesh->dim != 3) return bad(DG_ERR_ARG, "dim must be 2 or 3");
+  if (mesh->order < 1 || mesh->order > 4) return bad(DG_ERR_ARG, "order must be 1..4");
+  if (precision != DG_FP64 && precision != DG_FP32) return bad(DG_ERR_ARG, "precision must be DG_FP64 or DG_FP32");
+  if (mesh->n_elems <= 0 || mesh->n_nodes <= 0) return bad(DG_ERR_ARG, "empty mesh");
+  if (mesh->n_groups < 0 || mesh->n_groups > 32) return bad(DG_ERR_ARG, "at most 32 boundary groups");
+  if (mesh->n_groups > 0 && (!mesh->group_bc || !mesh->group_offsets || !mesh->group_nodes))
+    return bad(DG_ERR_ARG, "null group arrays");
+  if (!(phys->rho0 > 0) || !(phys->c0 > 0)) return bad(DG_ERR_ARG, "rho0 and c0 must be positive");
+  auto* c = new dg_ctx;
+  c->dim = mesh->dim, c->order = mesh->order, c->prec = precision, c->device = device;
+  try {
+    c->re = dgref::build(c->dim, c->order);
+  } catch (const std::exception& e) {
+    delete c;
+    return bad(DG_ERR_ARG, e.what());
+  }
+  c->sh = dgk::shape_info(c->dim, c->order);
+  c->np = c->re.np, c->nf = c->re.nf, c->nfp = c->re.nfp, c->nv = c->dim + 1;
+  if (mesh->nodes_per_elem != c->np) {
+    delete c;
+    return bad(DG_ERR_ARG, "nodes_per_elem does not match dim/order");
+  }
+  c->E = mesh->n_elems, c->nnodes = mesh->n_nodes;
+  c->ntiles = (c->E + c->sh.et - 1) / c->sh.et;
+  c->Epad = c->ntiles * c->sh.et;
+  if (c->Epad >= (int64_t)1 << 31) {
+    delete c;
+    return bad(DG_ERR_ARG, "too many elements");
+  }
+  c->tsize = precision == DG_FP32 ? 4 : 8;
+  for (int d = 0; d < 3; ++d) c->ph.v0[d] = phys->v0[d];
+  c->ph.rho0 = phys->rho0, c->ph.c0 = phys->c0;
+  c->ph.rhoc2 = phys->rho0 * phys->c0 * phys->c0;
+  c->ph.inv_rho0 = 1.0 / phys->rho0;
+  c->ph.half_c0 = 0.5 * phys->c0;
+  c->c0sq = phys->c0 * phys->c0;
+  // node permutation from element 0 (checked on every element by the setup)
+  {
+    const int D = c->dim, np = c->np;
+    for (int64_t k = 0; k < (int64_t)c->E * np; ++k)
+      if (mesh->elem_nodes[k] < 0 || mesh->elem_nodes[k] >= mesh->n_nodes) {
+        delete c;
+        return bad(DG_ERR_ARG, "element node index out of range");
+      }
+    const int64_t* en = mesh->elem_nodes;
+    const double* x0 = mesh->xyz + 3 * en[0];
+    double J[3][3] = {{0}}, Gi[3][3] = {{0}};
+    for (int k = 0; k < D; ++k)
+      for (int d = 0; d < D; ++d) J[d][k] = mesh->xyz[3 * en[k + 1] + d] - x0[d];
+    if (D == 2) {
+      double dt = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      Gi[0][0] = J[1][1] / dt, Gi[0][1] = -J[0][1] / dt, Gi[1][0] = -J[1][0] / dt, Gi[1][1] = J[0][0] / dt;
+    } else {
+      double dt = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                  J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      Gi[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / dt;
+      Gi[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / dt;
+      Gi[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / dt;
+      Gi[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / dt;
+      Gi[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / dt;
+      Gi[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / dt;
+      Gi[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / dt;
+      Gi[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / dt;
+      Gi[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / dt;
+    }
+    c->perm_c2i.assign(np, -1);
+    std::vector<int> used(np, 0);
+    for (int n = 0; n < np; ++n) {
+      int lat[3] = {0, 0, 0};
+      for (int r = 0; r < D; ++r) {
+        double xi = 0.0;
+        for (int d = 0; d < D; ++d) xi += Gi[r][d] * (mesh->xyz[3 * en[n] + d] - x0[d]);
+        lat[r] = (int)std::lround(xi * c->order);
+      }
+      int idx = dgref::lattice_index(c->re, lat);
+      if (idx < 0 || used[idx]) {
+        delete c;
+        return bad(DG_ERR_MESH, "element 0 nodes do not form a straight-sided Lagrange lattice");
+      }
+      used[idx] = 1;
+      c->perm_c2i[n] = idx;
+    }
+  }
+  // device, stream, buffers
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    std::string m = std::string("CUDA: ") + cudaGetErrorString(e);
+    dg_destroy(c);
+    return bad(DG_ERR_CUDA, m);
+  }
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, c->stream);
+  int rc = dgc::run_setup(c, mesh);
+  if (rc != DG_OK) {
+    std::string m = c->err;
+    dg_destroy(c);
+    return bad(rc, m);
+  }
+  // blocks per SM for the persistent stage kernel
+  int bps = 1;
+  if (c->prec == DG_FP32)
+    bps = c->dim == 2 ? dgk::blocks_per_sm_f32_2d(c->order) : dgk::blocks_per_sm_f32_3d(c->order);
+  else
+    bps = c->dim == 2 ? dgk::blocks_per_sm_f64_2d(c->order) : dgk::blocks_per_sm_f64_3d(c->order);
+  c->grid = (int)std::min<int64_t>(c->ntiles, (int64_t)bps * c->num_sms);
+  const size_t ts = c->tsize;
+  const int64_t nstate = (int64_t)c->nv * c->Epad * c->np;
+  void** bufs[6] = {&c->u, &c->acc, &c->y0, &c->y1, &c->snap, &c->kbuf};
+  for (auto b : bufs) {
+    e = dgc::dev_alloc(c, b, nstate * ts);
+    if (e == cudaSuccess) e = cudaMemsetAsync(*b, 0, nstate * ts, c->stream);
+    if (e != cudaSuccess) break;
+  }
+  std::vector<short> fm(c->re.fmask.begin(), c->re.fmask.end()), nb(c->re.nbrnode.begin(), c->re.nbrnode.end());
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->fmask, fm.size() * sizeof(short));
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->nbrnode, nb.size() * sizeof(short));
+  if (e == cudaSuccess) e = cudaMemcpy(c->fmask, fm.data(), fm.size() * sizeof(short), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->nbrnode, nb.data(), nb.size() * sizeof(short), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    if (c->prec == DG_FP32) {
+      std::vector<float> Dt, L;
+      to_dev_ops(c->re, Dt, L);
+      e = dgc::dev_alloc(c, &c->Dt, Dt.size() * 4);
+      if (e == cudaSuccess) e = dgc::dev_alloc(c, &c->LIFT, L.size() * 4);
+      if (e == cudaSuccess) e = cudaMemcpy(c->Dt, Dt.data(), Dt.size() * 4, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(c->LIFT, L.data(), L.size() * 4, cudaMemcpyHostToDevice);
+    } else {
+      std::vector<double> Dt, L;
+      to_dev_ops(c->re, Dt, L);
+      e = dgc::dev_alloc(c, &c->Dt, Dt.size() * 8);
+      if (e == cudaSuccess) e = dgc::dev_alloc(c, &c->LIFT, L.size() * 8);
+      if (e == cudaSuccess) e = cudaMemcpy(c->Dt, Dt.data(), Dt.size() * 8, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(c->LIFT, L.data(), L.size() * 8, cudaMemcpyHostToDevice);
+    }
+  }
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_perm, c->np * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_perm, c->perm_c2i.data(), c->np * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_ref, 4 * c->E * c->np * sizeof(double));
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->partials, std::max(c->grid, 2 * c->num_sms) * 5 * sizeof(double));
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_step, 2 * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_step, 0, 2 * sizeof(int64_t), c->stream);
+  cudaEventRecord(t1, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    std::string m = std::string("CUDA: ") + cudaGetErrorString(e);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    dg_destroy(c);
+    return bad(DG_ERR_CUDA, m);
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  c->info.dim = c->dim, c->info.order = c->order, c->info.nodes_per_elem = c->np, c->info.n_var = c->nv;
+  c->info.precision = c->prec, c->info.n_elems = c->E, c->info.n_faces = c->n_faces;
+  c->info.n_boundary_faces = c->n_bfaces;
+  c->info.device_bytes = c->device_bytes;
+  c->info.setup_ms = ms;
+  *out = c;
+  return DG_OK;
+}
+
+int dg_destroy(dg_ctx* c) {
+  if (!c) return DG_OK;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (void* p : c->allocs) cudaFree(p);
+  void* extra[] = {c->d_res, c->d_obs, c->d_src_dof, c->d_src_off, c->d_src_ids, c->d_srcval,
+                   c->d_obs_dof, c->d_obs_off, c->d_obs_w};
+  for (void* p : extra)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return DG_OK;
+}
+
+int dg_get_info(const dg_ctx* c, dg_info_t* info) {
+  if (!c || !info) return DG_ERR_ARG;
+  *info = c->info;
+  info->device_bytes = c->device_bytes;
+  return DG_OK;
+}
+
+int dg_set_state(dg_ctx* c, const double* u) {
+  if (!c || !u) return DG_ERR_ARG;
+  const int64_t n = 4 * c->E * c->np;
+  if (c->dim == 2)
+    for (int64_t i = 3 * c->E * c->np; i < n; ++i)
+      if (u[i] != 0.0) return fail(c, DG_ERR_ARG, "2-D state must have vz = 0");
+  CK(c, cudaMemcpyAsync(c->d_ref, u, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int64_t m = (int64_t)c->nv * c->E * c->np;
+  if (c->prec == DG_FP32)
+    k_ref_to_int<float><<<nblk(m, 256), 256, 0, c->stream>>>(c->d_ref, (float*)c->u, c->d_perm, c->E, c->np, c->nv,
+                                                             c->Epad * c->np);
+  else
+    k_ref_to_int<double><<<nblk(m, 256), 256, 0, c->stream>>>(c->d_ref, (double*)c->u, c->d_perm, c->E, c->np, c->nv,
+                                                              c->Epad * c->np);
+  CK(c, cudaGetLastError());
+  CK(c, cudaStreamSynchronize(c->stream));
+  return DG_OK;
+}
+
+int dg_get_state(dg_ctx* c, double* u) {
+  if (!c || !u) return DG_ERR_ARG;
+  const int64_t n = 4 * c->E * c->np;
+  if (c->prec == DG_FP32)
+    k_int_to_ref<float><<<nblk(n, 256), 256, 0, c->stream>>>((const float*)c->u, c->d_ref, c->d_perm, c->E, c->np,
+                                                             c->nv, c->Epad * c->np);
+  else
+    k_int_to_ref<double><<<nblk(n, 256), 256, 0, c->stream>>>((const double*)c->u, c->d_ref, c->d_perm, c->E, c->np,
+                                                              c->nv, c->Epad * c->np);
+  CK(c, cudaGetLastError());
+  CK(c, cudaMemcpyAsync(u, c->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return DG_OK;
+}
+
+int dg_set_sources(dg_ctx* c, int n_src, const int64_t* offsets, const int64_t* dofs) {
+  if (!c || n_src < 0 || (n_src > 0 && (!offsets || !dofs))) return DG_ERR_ARG;
+  // unique internal dofs, each with the ordered list of sources covering it
+  std::map<int64_t, std::vector<int>> cover;
+  const int64_t ndof = c->E * c->np;
+  for (int s = 0; s < n_src; ++s)
+    for (int64_t k = offsets[s]; k < offsets[s + 1]; ++k) {
+      int64_t d = dofs[k];
+      if (d < 0 || d >= ndof) return fail(c, DG_ERR_ARG, "source dof out of range");
+      int64_t e = d / c->np;
+      int n = (int)(d - e * c->np);
+      int64_t idof = e * c->np + c->perm_c2i[n];
+      auto& v = cover[idof];
+      if (v.empty() || v.back() != s) v.push_back(s);
+    }
+  std::vector<int64_t> hd;
+  std::vector<int> ho(1, 0), hi;
+  for (auto& kv : cover) {
+    hd.push_back(kv.first);
+    for (int s : kv.second) hi.push_back(s);
+    ho.push_back((int)hi.size());
+  }
+  for (void* p : {(void*)c->d_src_dof, (void*)c->d_src_off, (void*)c->d_src_ids})
+    if (p) cudaFree(p);
+  c->d_src_dof = nullptr, c->d_src_off = nullptr, c->d_src_ids = nullptr;
+  c->n_src = n_src;
+  c->n_src_dofs = (int64_t)hd.size();
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  if (hd.empty()) return DG_OK;
+  CK(c, cudaMalloc(&c->d_src_dof, hd.size() * sizeof(int64_t)));
+  CK(c, cudaMalloc(&c->d_src_off, ho.size() * sizeof(int)));
+  CK(c, cudaMalloc(&c->d_src_ids, hi.size() * sizeof(int)));
+  CK(c, cudaMemcpy(c->d_src_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->d_src_off, ho.data(), ho.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->d_src_ids, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return DG_OK;
+}
+
+int dg_set_source_values(dg_ctx* c, int64_t n_steps, const double* values) {
+  if (!c || n_steps < 0 || (n_steps > 0 && c->n_src > 0 && !values)) return DG_ERR_ARG;
+  if (c->d_srcval) cudaFree(c->d_srcval), c->d_srcval = nullptr;
+  c->srcval_steps = 0;
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  if (n_steps == 0 || c->n_src == 0) return DG_OK;
+  CK(c, cudaMalloc(&c->d_srcval, n_steps * c->n_src * sizeof(double)));
+  CK(c, cudaMemcpy(c->d_srcval, values, n_steps * c->n_src * sizeof(double), cudaMemcpyHostToDevice));
+  c->srcval_steps = n_steps;
+  return DG_OK;
+}
+
+int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t* dofs, const double* weights) {
+  if (!c || n_obs < 0 || (n_obs > 0 && (!offsets || !dofs || !weights))) return DG_ERR_ARG;
+  for (void* p : {(void*)c->d_obs_dof, (void*)c->d_obs_off, (void*)c->d_obs_w})
+    if (p) cudaFree(p);
+  c->d_obs_dof = nullptr, c->d_obs_off = nullptr, c->d_obs_w = nullptr;
+  c->n_obs = n_obs;
+  if (c->d_obs) cudaFree(c->d_obs), c->d_obs = nullptr;
+  if (c->d_res) cudaFree(c->d_res), c->d_res = nullptr;
+  c->out_cap = 0;
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  if (n_obs == 0) return DG_OK;
+  int64_t total = offsets[n_obs];
+  std::vector<int64_t> hd(std::max<int64_t>(total, 1));
+  const int64_t ndof = c->E * c->np;
+  for (int64_t k = 0; k < total; ++k) {
+    int64_t d = dofs[k];
+    if (d < 0 || d >= ndof) return fail(c, DG_ERR_ARG, "observer dof out of range");
+    int64_t e = d / c->np;
+    hd[k] = e * c->np + c->perm_c2i[d - e * c->np];
+  }
+  CK(c, cudaMalloc(&c->d_obs_dof, hd.size() * sizeof(int64_t)));
+  CK(c, cudaMalloc(&c->d_obs_off, (n_obs + 1) * sizeof(int64_t)));
+  CK(c, cudaMalloc(&c->d_obs_w, std::max<int64_t>(total, 1) * sizeof(double)));
+  CK(c, cudaMemcpy(c->d_obs_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpy(c->d_obs_off, offsets, (n_obs + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+  if (total > 0) CK(c, cudaMemcpy(c->d_obs_w, weights, total * sizeof(double), cudaMemcpyHostToDevice));
+  return DG_OK;
+}
+
+int dg_snapshot(dg_ctx* c) {
+  if (!c) return DG_ERR_ARG;
+  CK(c, cudaMemcpyAsync(c->snap, c->u, (size_t)c->nv * c->Epad * c->np * c->tsize, cudaMemcpyDeviceToDevice,
+                        c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return DG_OK;
+}
+
+int dg_run(dg_ctx* c, int64_t n_steps, double dt, double* residuals, double* obs) {
+  return run_steps(c, 0, n_steps, dt, residuals, obs);
+}
+
+int dg_run_euler(dg_ctx* c, int64_t n_steps, double dt, double* residuals, double* obs) {
+  return run_steps(c, 1, n_steps, dt, residuals, obs);
+}
+
+int64_t dg_step_index(const dg_ctx* c) { return c ? c->step : -1; }
+
+int dg_set_step_index(dg_ctx* c, int64_t step) {
+  if (!c || step < 0) return DG_ERR_ARG;
+  c->step = step;
+  return DG_OK;
+}
+
+int dg_rhs(dg_ctx* c, const double* u, double dt, double* k) {
+  if (!c || !u || !k) return DG_ERR_ARG;
+  const int64_t n = 4 * c->E * c->np, m = (int64_t)c->nv * c->E * c->np, stride = c->Epad * c->np;
+  CK(c, cudaMemcpyAsync(c->d_ref, u, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->prec == DG_FP32)
+    k_ref_to_int<float><<<nblk(m, 256), 256, 0, c->stream>>>(c->d_ref, (float*)c->y1, c->d_perm, c->E, c->np, c->nv,
+                                                             stride);
+  else
+    k_ref_to_int<double><<<nblk(m, 256), 256, 0, c->stream>>>(c->d_ref, (double*)c->y1, c->d_perm, c->E, c->np,
+                                                              c->nv, stride);
+  CK(c, cudaGetLastError());
+  CK(c, launch_stage(c, 0, c->y1, nullptr, c->kbuf, dt));
+  if (c->prec == DG_FP32)
+    k_int_to_ref<float><<<nblk(n, 256), 256, 0, c->stream>>>((const float*)c->kbuf, c->d_ref, c->d_perm, c->E, c->np,
+                                                             c->nv, stride);
+  else
+    k_int_to_ref<double><<<nblk(n, 256), 256, 0, c->stream>>>((const double*)c->kbuf, c->d_ref, c->d_perm, c->E,
+                                                              c->np, c->nv, stride);
+  CK(c, cudaGetLastError());
+  CK(c, cudaMemcpyAsync(k, c->d_ref, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return DG_OK;
+}
+
+int dg_cell_means(dg_ctx* c, double* p, double* rho, double* v) {
+  if (!c) return DG_ERR_ARG;
+  std::vector<double> h(c->E * 5);
+  if (c->prec == DG_FP32)
+    k_cell_means<float><<<nblk(c->E, 128), 128, 0, c->stream>>>((const float*)c->u, c->d_perm, c->E, c->np, c->nv,
+                                                                c->Epad * c->np, c->c0sq, c->d_ref);
+  else
+    k_cell_means<double><<<nblk(c->E, 128), 128, 0, c->stream>>>((const double*)c->u, c->d_perm, c->E, c->np, c->nv,
+                                                                 c->Epad * c->np, c->c0sq, c->d_ref);
+  CK(c, cudaGetLastError());
+  CK(c, cudaMemcpyAsync(h.data(), c->d_ref, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int64_t e = 0; e < c->E; ++e) {
+    if (p) p[e] = h[e * 5];
+    if (rho) rho[e] = h[e * 5 + 1];
+    if (v)
+      for (int d = 0; d < 3; ++d) v[e * 3 + d] = h[e * 5 + 2 + d];
+  }
+  return DG_OK;
+}
+
+int dg_face_info(dg_ctx* c, int64_t* nbr, int* penalty, int* bc) {
+  if (!c) return DG_ERR_ARG;
+  const int reci = c->sh.reci, nf = c->nf;
+  std::vector<int> gi(c->E * reci);
+  CK(c, cudaMemcpy(gi.data(), c->geoI, gi.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> bcodes(std::max<int64_t>(c->n_bfaces, 1));
+  if (c->n_bfaces > 0) CK(c, cudaMemcpy(bcodes.data(), c->d_bcode, c->n_bfaces * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int64_t e = 0; e < c->E; ++e)
+    for (int lf = 0; lf < nf; ++lf) {
+      int nb = gi[e * reci + lf], code = gi[e * reci + nf + lf];
+      bool b = code & dgk::kCodeBoundary;
+      if (nbr) nbr[e * nf + lf] = b ? -1 : nb;
+      if (penalty) penalty[e * nf + lf] = b ? 0 : ((code & dgk::kCodeNegPenalty) ? -1 : 1);
+      if (bc) bc[e * nf + lf] = b ? bcodes[nb] : -1;
+    }
+  return DG_OK;
+}
+
+void* dg_stream(dg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int dg_bench_steps(dg_ctx* c, int64_t n_steps, double dt, int64_t flush_bytes, double* step_ms, double* kernel_ms) {
+  if (!c || n_steps <= 0 || !(dt > 0)) return DG_ERR_ARG;
+  int rc = ensure_out_cap(c, n_steps);
+  if (rc) return rc;
+  rc = build_graph(c, 0, dt);
+  if (rc) return rc;
+  unsigned* flush = nullptr;
+  int64_t nflush = flush_bytes / 4;
+  if (nflush > 0) CK(c, cudaMalloc(&flush, nflush * 4));
+  int64_t st[2] = {c->step, c->step};
+  CK(c, cudaMemcpyAsync(c->d_step, st, sizeof(st), cudaMemcpyHostToDevice, c->stream));
+  std::vector<cudaEvent_t> ev(2 * n_steps);
+  for (auto& x : ev) cudaEventCreate(&x);
+  for (int64_t i = 0; i < n_steps; ++i) {
+    if (flush) k_flush<<<2 * c->num_sms, 512, 0, c->stream>>>(flush, nflush, (unsigned)i);
+    cudaEventRecord(ev[2 * i], c->stream);
+    cudaGraphLaunch(c->graph, c->stream);
+    cudaEventRecord(ev[2 * i + 1], c->stream);
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  double tot = 0.0;
+  for (int64_t i = 0; i < n_steps; ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    tot += ms;
+  }
+  c->step += n_steps;
+  if (step_ms) *step_ms = tot / n_steps;
+  if (kernel_ms) {
+    // second pass without the graph: events around each stage launch
+    std::vector<cudaEvent_t> se(8 * n_steps);
+    for (auto& x : se) cudaEventCreate(&x);
+    st[0] = st[1] = c->step;
+    CK(c, cudaMemcpyAsync(c->d_step, st, sizeof(st), cudaMemcpyHostToDevice, c->stream));
+    for (int64_t i = 0; i < n_steps; ++i) {
+      if (flush) k_flush<<<2 * c->num_sms, 512, 0, c->stream>>>(flush, nflush, (unsigned)i);
+      cudaError_t err = enqueue_step(c, 0, dt, &se[8 * i]);
+      if (err != cudaSuccess) {
+        for (auto& x : se) cudaEventDestroy(x);
+        return fail(c, DG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(err));
+      }
+    }
+    CK(c, cudaStreamSynchronize(c->stream));
+    double kt = 0.0;
+    for (int64_t i = 0; i < 4 * n_steps; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, se[2 * i], se[2 * i + 1]);
+      kt += ms;
+    }
+    for (auto& x : se) cudaEventDestroy(x);
+    c->step += n_steps;
+    *kernel_ms = kt / n_steps;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (flush) cudaFree(flush);
+  return DG_OK;
+}
+
+}  // extern "C"

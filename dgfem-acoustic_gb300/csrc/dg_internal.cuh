@@ -1,0 +1,108 @@
+// Internal declarations shared by the CUDA translation units of the solver.
+//
+// Device data layout (all per-element arrays padded to Epad = tiles * ET):
+//   state   T [n_var][Epad*Np]  per variable, element-major, internal lattice
+//                               node order inside an element
+//   geoF    T [Epad][RECF]      G = d(xi)/dx (dim*dim), then per local face:
+//                               outward unit normal (dim) and sJ = J_f/|det J|
+//   geoI    int [Epad][RECI]    per local face: neighbour element (interior)
+//                               or boundary-face index; then per local face the
+//                               face code (neighbour local face, corner
+//                               permutation, penalty sign, boundary flag)
+//   bmat    T [n_bfaces][n_var*n_var]  boundary flux matrix (RKR or reflecting)
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace dgk {
+
+constexpr int kCodeLfMask = 0x3;       // neighbour local face
+constexpr int kCodePermShift = 2;      // corner permutation index (3 bits)
+constexpr int kCodePermMask = 0x7;
+constexpr int kCodeNegPenalty = 1 << 5;  // penalty sign s_f = -1
+constexpr int kCodeBoundary = 1 << 6;    // boundary face; nbr slot holds the boundary index
+
+// Compile-time shape of a (dim, order) pair.
+template <int D, int P>
+struct Shape {
+  static constexpr int NP = D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6;
+  static constexpr int NF = D + 1;
+  static constexpr int NFP = D == 2 ? P + 1 : (P + 1) * (P + 2) / 2;
+  static constexpr int NV = D + 1;
+  static constexpr int NPERM = D == 2 ? 2 : 6;
+  // threads per element: each owns a chunk of NC output nodes
+  static constexpr int NCMAX = D == 2 ? 6 : 5;
+  static constexpr int NSPLIT = (NP + NCMAX - 1) / NCMAX;
+  static constexpr int NC = (NP + NSPLIT - 1) / NSPLIT;
+  // elements per tile: a multiple of 4 (16-byte tile boundaries) with
+  // ET * NSPLIT a multiple of the warp size
+  static constexpr int ET = NSPLIT <= 2 ? 128 / NSPLIT : 32;
+  static constexpr int NT = ET * NSPLIT;  // threads per block
+  static constexpr int RECF_RAW = D * D + NF * (D + 1);
+  static constexpr int RECI = ((2 * NF) + 3) / 4 * 4;
+};
+
+template <int D, int P, typename T>
+struct ShapeT : Shape<D, P> {
+  static constexpr int VEC = 16 / sizeof(T);
+  static constexpr int RECF = (Shape<D, P>::RECF_RAW + VEC - 1) / VEC * VEC;
+};
+
+// Physical constants used by the kernels.
+struct Phys {
+  double v0[3];
+  double rho0, c0, rhoc2, inv_rho0, half_c0;
+};
+
+template <typename T>
+struct StageArgs {
+  const T* y_in;   // stage input
+  T* y_out;        // next stage input (stages 1-3)
+  T* u;            // state at step start (updated in stage 4)
+  T* acc;          // RK accumulator
+  const T* snap;   // residual reference (stage 4)
+  T* k_out;        // stage 0: dt*L(y_in)
+  double* partials;  // [gridDim][5] residual partial sums (stage 4)
+  const T* geoF;
+  const int* geoI;
+  const T* bmat;
+  const T* Dt;     // [D][NP(j)][NP(i)]
+  const T* LIFT;   // [NF*NFP(k)][NP(i)]
+  const short* fmask;   // [NF*NFP]
+  const short* nbrnode; // [NF*NPERM*NFP]
+  int64_t stride;  // Epad*NP
+  int ntiles;
+  int stage;       // 0: k only, 1..4: RK4 stages, 5: Euler (y_out = u + k)
+  double dt;
+  double c0sq;
+  Phys ph;
+};
+
+// Stage launchers and occupancy queries; defined in stage_{f32,f64}_{2,3}d.cu.
+cudaError_t launch_stage_f32_2d(int order, const StageArgs<float>& a, int grid, cudaStream_t s);
+cudaError_t launch_stage_f32_3d(int order, const StageArgs<float>& a, int grid, cudaStream_t s);
+cudaError_t launch_stage_f64_2d(int order, const StageArgs<double>& a, int grid, cudaStream_t s);
+cudaError_t launch_stage_f64_3d(int order, const StageArgs<double>& a, int grid, cudaStream_t s);
+int blocks_per_sm_f32_2d(int order);
+int blocks_per_sm_f32_3d(int order);
+int blocks_per_sm_f64_2d(int order);
+int blocks_per_sm_f64_3d(int order);
+
+// Host-side shape queries for a runtime (dim, order).
+struct ShapeInfo {
+  int np, nf, nfp, nv, nperm, et, nt, recf32, recf64, reci;
+};
+inline ShapeInfo shape_info(int dim, int order) {
+#define DGK_SHAPE(D, P)                                                                                  \
+  if (dim == D && order == P)                                                                            \
+    return ShapeInfo{Shape<D, P>::NP,     Shape<D, P>::NF,     Shape<D, P>::NFP,           Shape<D, P>::NV, \
+                     Shape<D, P>::NPERM,  Shape<D, P>::ET,     Shape<D, P>::NT,            ShapeT<D, P, float>::RECF, \
+                     ShapeT<D, P, double>::RECF, Shape<D, P>::RECI};
+  DGK_SHAPE(2, 1) DGK_SHAPE(2, 2) DGK_SHAPE(2, 3) DGK_SHAPE(2, 4)
+  DGK_SHAPE(3, 1) DGK_SHAPE(3, 2) DGK_SHAPE(3, 3) DGK_SHAPE(3, 4)
+#undef DGK_SHAPE
+  return ShapeInfo{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+}
+
+}  // namespace dgk

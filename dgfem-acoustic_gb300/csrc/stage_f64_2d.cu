@@ -1,0 +1,26 @@
+// Instantiations of the fused stage kernel: double, 2-D, orders 1..4.
+#include "stage.cuh"
+
+namespace dgk {
+
+cudaError_t launch_stage_f64_2d(int order, const StageArgs<double>& a, int grid, cudaStream_t s) {
+  switch (order) {
+    case 1: return launch_stage_impl<double, 2, 1>(a, grid, s);
+    case 2: return launch_stage_impl<double, 2, 2>(a, grid, s);
+    case 3: return launch_stage_impl<double, 2, 3>(a, grid, s);
+    case 4: return launch_stage_impl<double, 2, 4>(a, grid, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int blocks_per_sm_f64_2d(int order) {
+  switch (order) {
+    case 1: return blocks_per_sm_impl<double, 2, 1>();
+    case 2: return blocks_per_sm_impl<double, 2, 2>();
+    case 3: return blocks_per_sm_impl<double, 2, 3>();
+    case 4: return blocks_per_sm_impl<double, 2, 4>();
+  }
+  return 1;
+}
+
+}  // namespace dgk

@@ -1,0 +1,216 @@
+"""ctypes binding of the GPU solver C ABI (include/dgfem_gb300.h).
+
+The binding loads the in-tree libdgfem_gb300.so and fails loudly when it is
+missing or when no CUDA device is usable; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libdgfem_gb300.so")
+_lib = None
+
+DG_FP64, DG_FP32 = 0, 1
+ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFINITE", 5: "DG_ERR_TIMEOUT"}
+
+# Every entry point declared in include/dgfem_gb300.h.
+SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
+           "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
+           "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
+           "dg_bench_steps"]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("nodes_per_elem", C.c_int),
+                ("n_nodes", C.c_int64), ("xyz", C.POINTER(C.c_double)),
+                ("n_elems", C.c_int64), ("elem_nodes", C.POINTER(C.c_int64)),
+                ("n_groups", C.c_int), ("group_bc", C.POINTER(C.c_int)),
+                ("group_offsets", C.POINTER(C.c_int64)), ("group_nodes", C.POINTER(C.c_int64))]
+
+
+class Phys(C.Structure):
+    _fields_ = [("v0", C.c_double * 3), ("rho0", C.c_double), ("c0", C.c_double)]
+
+
+class Info(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("nodes_per_elem", C.c_int), ("n_var", C.c_int),
+                ("precision", C.c_int), ("n_elems", C.c_int64), ("n_faces", C.c_int64),
+                ("n_boundary_faces", C.c_int64), ("penalty_sign_hist", C.c_int64 * 2),
+                ("device_bytes", C.c_int64), ("setup_ms", C.c_double)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("GPU solver library not built: %s (run __graft_entry__.build())" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        P, D, I64 = C.POINTER, C.c_double, C.c_int64
+        L.dg_create.argtypes = [P(MeshDesc), P(Phys), C.c_int, C.c_int, P(C.c_void_p)]
+        L.dg_destroy.argtypes = [C.c_void_p]
+        L.dg_last_error.argtypes = [C.c_void_p]
+        L.dg_last_error.restype = C.c_char_p
+        L.dg_get_info.argtypes = [C.c_void_p, P(Info)]
+        L.dg_set_state.argtypes = [C.c_void_p, P(D)]
+        L.dg_get_state.argtypes = [C.c_void_p, P(D)]
+        L.dg_set_sources.argtypes = [C.c_void_p, C.c_int, P(I64), P(I64)]
+        L.dg_set_source_values.argtypes = [C.c_void_p, I64, P(D)]
+        L.dg_set_observers.argtypes = [C.c_void_p, C.c_int, P(I64), P(I64), P(D)]
+        L.dg_snapshot.argtypes = [C.c_void_p]
+        L.dg_run.argtypes = [C.c_void_p, I64, D, P(D), P(D)]
+        L.dg_run_euler.argtypes = [C.c_void_p, I64, D, P(D), P(D)]
+        L.dg_step_index.argtypes = [C.c_void_p]
+        L.dg_step_index.restype = I64
+        L.dg_set_step_index.argtypes = [C.c_void_p, I64]
+        L.dg_rhs.argtypes = [C.c_void_p, P(D), D, P(D)]
+        L.dg_cell_means.argtypes = [C.c_void_p, P(D), P(D), P(D)]
+        L.dg_face_info.argtypes = [C.c_void_p, P(I64), P(C.c_int), P(C.c_int)]
+        L.dg_stream.argtypes = [C.c_void_p]
+        L.dg_stream.restype = C.c_void_p
+        L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64)) if a is not None else None
+
+
+def _csr(lists, dtype=np.int64):
+    off = np.zeros(len(lists) + 1, dtype=np.int64)
+    for i, l in enumerate(lists):
+        off[i + 1] = off[i] + len(l)
+    flat = np.concatenate([np.asarray(l, dtype=dtype) for l in lists]) if off[-1] > 0 else np.zeros(1, dtype)
+    return off, np.ascontiguousarray(flat)
+
+
+class SolverError(RuntimeError):
+    pass
+
+
+class Solver:
+    """One solver context on one GPU (see include/dgfem_gb300.h)."""
+
+    def __init__(self, mesh, v0=(0.0, 0.0, 0.0), rho0=1.0, c0=1.0, precision=DG_FP64, device=0):
+        L = lib()
+        xyz = np.ascontiguousarray(mesh["xyz"], dtype=np.float64)
+        en = np.ascontiguousarray(mesh["elem_nodes"], dtype=np.int64)
+        groups = mesh.get("groups", [])
+        gbc = np.array([g[0] for g in groups] or [0], dtype=np.int32)
+        goff, gn = _csr([g[1] for g in groups])
+        d = MeshDesc()
+        d.dim, d.order, d.nodes_per_elem = mesh["dim"], mesh["order"], en.shape[1]
+        d.n_nodes, d.xyz = xyz.shape[0], _dp(xyz)
+        d.n_elems, d.elem_nodes = en.shape[0], _ip(en)
+        d.n_groups, d.group_bc = len(groups), gbc.ctypes.data_as(C.POINTER(C.c_int))
+        d.group_offsets, d.group_nodes = _ip(goff), _ip(gn)
+        ph = Phys()
+        ph.v0 = (C.c_double * 3)(*v0)
+        ph.rho0, ph.c0 = rho0, c0
+        h = C.c_void_p()
+        rc = L.dg_create(C.byref(d), C.byref(ph), precision, device, C.byref(h))
+        if rc != 0:
+            raise SolverError("dg_create: %s: %s" % (ERRORS.get(rc, rc), L.dg_last_error(None).decode()))
+        self.h = h
+        self.E, self.np_, self.dim = en.shape[0], en.shape[1], mesh["dim"]
+        self.n_obs = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise SolverError("%s: %s: %s" % (what, ERRORS.get(rc, rc), lib().dg_last_error(self.h).decode()))
+
+    @property
+    def ndof(self):
+        return self.E * self.np_
+
+    def info(self):
+        i = Info()
+        self._ck(lib().dg_get_info(self.h, C.byref(i)), "dg_get_info")
+        return {k: (tuple(getattr(i, k)) if k == "penalty_sign_hist" else getattr(i, k)) for k, _ in Info._fields_}
+
+    def set_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(4, self.ndof)
+        self._ck(lib().dg_set_state(self.h, _dp(u)), "dg_set_state")
+
+    def get_state(self):
+        u = np.zeros((4, self.ndof))
+        self._ck(lib().dg_get_state(self.h, _dp(u)), "dg_get_state")
+        return u
+
+    def rhs(self, u, dt):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(4, self.ndof)
+        k = np.zeros_like(u)
+        self._ck(lib().dg_rhs(self.h, _dp(u), dt, _dp(k)), "dg_rhs")
+        return k
+
+    def set_sources(self, dof_lists):
+        off, flat = _csr(dof_lists)
+        self._ck(lib().dg_set_sources(self.h, len(dof_lists), _ip(off), _ip(flat)), "dg_set_sources")
+
+    def set_source_values(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._ck(lib().dg_set_source_values(self.h, v.shape[0], _dp(v)), "dg_set_source_values")
+
+    def set_observers(self, dof_lists, weight_lists):
+        off, flat = _csr(dof_lists)
+        _, w = _csr(weight_lists, np.float64)
+        self._ck(lib().dg_set_observers(self.h, len(dof_lists), _ip(off), _ip(flat), _dp(w)), "dg_set_observers")
+        self.n_obs = len(dof_lists)
+
+    def snapshot(self):
+        self._ck(lib().dg_snapshot(self.h), "dg_snapshot")
+
+    def run(self, n_steps, dt, euler=False):
+        res = np.zeros((max(n_steps, 1), 5))
+        obs = np.zeros((max(n_steps, 1), max(self.n_obs, 1), 4))
+        fn = lib().dg_run_euler if euler else lib().dg_run
+        self._ck(fn(self.h, n_steps, dt, _dp(res), _dp(obs)), "dg_run")
+        return res[:n_steps], obs[:n_steps, :self.n_obs]
+
+    @property
+    def step(self):
+        return lib().dg_step_index(self.h)
+
+    @step.setter
+    def step(self, s):
+        self._ck(lib().dg_set_step_index(self.h, s), "dg_set_step_index")
+
+    def cell_means(self):
+        p, rho, v = np.zeros(self.E), np.zeros(self.E), np.zeros((self.E, 3))
+        self._ck(lib().dg_cell_means(self.h, _dp(p), _dp(rho), _dp(v)), "dg_cell_means")
+        return p, rho, v
+
+    def face_info(self):
+        nf = self.dim + 1
+        nbr = np.zeros(self.E * nf, np.int64)
+        pen = np.zeros(self.E * nf, np.int32)
+        bc = np.zeros(self.E * nf, np.int32)
+        self._ck(lib().dg_face_info(self.h, _ip(nbr), pen.ctypes.data_as(C.POINTER(C.c_int)),
+                                    bc.ctypes.data_as(C.POINTER(C.c_int))), "dg_face_info")
+        return dict(nbr=nbr.reshape(-1, nf), penalty=pen.reshape(-1, nf), bc=bc.reshape(-1, nf))
+
+    def stream(self):
+        return lib().dg_stream(self.h)
+
+    def bench_steps(self, n_steps, dt, flush_bytes=0, kernel_time=True):
+        sm, km = C.c_double(), C.c_double()
+        self._ck(lib().dg_bench_steps(self.h, n_steps, dt, flush_bytes, C.byref(sm),
+                                      C.byref(km) if kernel_time else None), "dg_bench_steps")
+        return sm.value, (km.value if kernel_time else None)

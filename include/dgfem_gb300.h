@@ -1,0 +1,143 @@
+/*
+ * dgfem_gb300.h — C ABI of the GB300-native DG solver core.
+ *
+ * The reference (DGFEM-Acoustic) has no plugin API: its seam is the
+ * in-process call solver::rungeKutta(u, mesh, config) (include/solver.h:25,
+ * src/solver.cpp:311) on a Mesh built by Mesh::Mesh(config)
+ * (src/Mesh.cpp:20-686), driven by the dgalerkin executable
+ * (src/dgalerkin.cpp:14-85). This ABI splits that call into the pieces a host
+ * driver (the project's dgalerkin) needs, with plain C types only:
+ *
+ *   dg_create           replaces Mesh::Mesh + Mesh::precomputeMassMatrix
+ *                       (src/Mesh.cpp:20-724): GPU FP64 setup of geometry,
+ *                       face connectivity, normals, penalty signs, BC codes
+ *                       and boundary matrices (RKR, Mesh.cpp:619-666)
+ *   dg_set_state / dg_get_state
+ *                       the solution vector u[4][E*Np] of src/dgalerkin.cpp:51
+ *                       (per-variable, element-major, the mesh's local node
+ *                       order); vz is carried as zero in 2-D
+ *   dg_set_sources / dg_set_source_values
+ *                       source node sets (src/solver.cpp:339-358) and the
+ *                       per-step values written by the hard overwrite
+ *                       (src/solver.cpp:455-483)
+ *   dg_set_observers    observer node sets and IDW weights (src/solver.cpp:360-383)
+ *   dg_snapshot         the residual reference copy taken at output steps
+ *                       (src/solver.cpp:421-439)
+ *   dg_run              n time steps of classic RK4 (src/solver.cpp:413-574):
+ *                       source injection, four RHS stages (Mesh::updateFlux,
+ *                       numStep: src/Mesh.cpp:734-975, src/solver.cpp:38-57),
+ *                       the combine, the residuals and observer samples
+ *   dg_run_euler        n steps of forward Euler (src/solver.cpp:153-302)
+ *   dg_rhs              one numStep with beta = 0 after updateFlux:
+ *                       k = dt M^-1 (S - F) (src/solver.cpp:38-57)
+ *   dg_cell_means       element means written to the VTU files (src/Mesh.cpp:1196-1212)
+ *
+ * Conventions: every call returns DG_OK (0) or an error code; nothing aborts
+ * or throws. dg_last_error(ctx) returns the message of the last failure on
+ * ctx (ctx may be NULL for dg_create failures). One context owns one CUDA
+ * stream and all its device memory; a context is not thread-safe, distinct
+ * contexts may be used concurrently. Device memory is allocated in dg_create,
+ * dg_set_sources, dg_set_observers and on the first dg_run that needs more
+ * per-step output room.
+ */
+#ifndef DGFEM_GB300_H
+#define DGFEM_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DG_OK = 0,
+  DG_ERR_ARG = 1,       /* invalid argument or call order */
+  DG_ERR_CUDA = 2,      /* CUDA runtime error (no device, out of memory, launch failure) */
+  DG_ERR_MESH = 3,      /* unsupported or inconsistent mesh (curved, non-conforming, ...) */
+  DG_ERR_NONFINITE = 4, /* NaN/Inf detected in the state */
+  DG_ERR_TIMEOUT = 5    /* a bounded device wait gave up */
+};
+
+enum { DG_FP64 = 0, DG_FP32 = 1 };
+
+typedef struct dg_ctx dg_ctx;
+
+typedef struct {
+  int dim;            /* 2 (triangles) or 3 (tetrahedra) */
+  int order;          /* Lagrange order 1..4 */
+  int nodes_per_elem; /* Np */
+  int64_t n_nodes;
+  const double* xyz;         /* [n_nodes][3] node coordinates */
+  int64_t n_elems;
+  const int64_t* elem_nodes; /* [n_elems][Np] node indices; corners first (Gmsh order) */
+  /* boundary physical groups with a BC type, in ascending physical tag order
+   * (the order in which src/Mesh.cpp:582-605 applies them; last match wins) */
+  int n_groups;                 /* <= 32 */
+  const int* group_bc;          /* 1 = Reflecting, 0 = Absorbing */
+  const int64_t* group_offsets; /* [n_groups+1] */
+  const int64_t* group_nodes;   /* node indices of each group */
+} dg_mesh_desc;
+
+typedef struct {
+  double v0[3]; /* mean flow */
+  double rho0;
+  double c0;
+} dg_phys;
+
+typedef struct {
+  int dim, order, nodes_per_elem, n_var, precision;
+  int64_t n_elems, n_faces, n_boundary_faces;
+  int64_t penalty_sign_hist[2]; /* interior faces with s_f = -1, +1 */
+  int64_t device_bytes;
+  double setup_ms;
+} dg_info_t;
+
+int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out);
+int dg_destroy(dg_ctx* ctx);
+const char* dg_last_error(const dg_ctx* ctx);
+int dg_get_info(const dg_ctx* ctx, dg_info_t* info);
+
+int dg_set_state(dg_ctx* ctx, const double* u);
+int dg_get_state(dg_ctx* ctx, double* u);
+
+/* Source node sets: dofs are e*Np + n in the mesh's local node order.
+ * Sources are applied in index order; a later active source overwrites an
+ * earlier one on shared nodes. */
+int dg_set_sources(dg_ctx* ctx, int n_src, const int64_t* offsets, const int64_t* dofs);
+/* values[step][src] for global steps [0, n_steps); NaN = source inactive at that step */
+int dg_set_source_values(dg_ctx* ctx, int64_t n_steps, const double* values);
+/* Observer node sets with their IDW weights w = 1/(d^2 + 1e-12). */
+int dg_set_observers(dg_ctx* ctx, int n_obs, const int64_t* offsets, const int64_t* dofs, const double* weights);
+
+int dg_snapshot(dg_ctx* ctx);
+/* Runs n_steps RK4 steps from the current global step index. residuals
+ * [n_steps][5] (p, rho, vx, vy, vz) and obs [n_steps][n_obs][4] (p, vx, vy, vz)
+ * are filled when non-NULL. */
+int dg_run(dg_ctx* ctx, int64_t n_steps, double dt, double* residuals, double* obs);
+int dg_run_euler(dg_ctx* ctx, int64_t n_steps, double dt, double* residuals, double* obs);
+int64_t dg_step_index(const dg_ctx* ctx);
+int dg_set_step_index(dg_ctx* ctx, int64_t step);
+
+/* k = dt * M^-1 (S - F) of state u (both [4][E*Np]); the context state is unchanged. */
+int dg_rhs(dg_ctx* ctx, const double* u, double dt, double* k);
+/* element means of p, p/c0^2 and v ([E], [E], [E][3]) */
+int dg_cell_means(dg_ctx* ctx, double* p, double* rho, double* v);
+
+/* Per element local face (n_elems x (dim+1), local faces in Gmsh order):
+ * neighbour element (-1 on the boundary), penalty sign s_f (0 on the
+ * boundary) and BC code (1 reflecting, 0 absorbing, -1 interior). */
+int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
+
+/* The CUDA stream (cudaStream_t) all work of ctx is issued on. */
+void* dg_stream(dg_ctx* ctx);
+/* Timed RK4 steps for benchmarking: runs n_steps with the per-step graph and
+ * returns the per-step device time from CUDA events on ctx's stream; when
+ * kernel_ms is non-NULL also the summed time of the four stage kernels,
+ * timed with events around each stage launch in a second pass. flush_bytes > 0
+ * writes a scratch buffer of that size between steps (outside the timing). */
+int dg_bench_steps(dg_ctx* ctx, int64_t n_steps, double dt, int64_t flush_bytes, double* step_ms,
+                   double* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

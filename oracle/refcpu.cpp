@@ -524,13 +524,18 @@ void RefMesh::setup(const refcpu_input* input) {
       return lattice[n * D + v - 1];
     };
     for (int k = 0; k < D; ++k) m_locFaceNodes[lf * Nfp + cnt++] = corners[k];
-    for (int n = 0; n < Np; ++n) {
-      bool corner = n < nc;
-      if (corner) continue;
+    // remaining face nodes ordered by their face coordinates, so that every
+    // local face has the same node arrangement (one face basis serves all)
+    std::vector<std::pair<int, int>> rest;  // (sort key, node)
+    for (int n = nc; n < Np; ++n)
       if (bary(n, opp) == 0) {
-        if (cnt >= Nfp) throw std::runtime_error("too many face nodes");
-        m_locFaceNodes[lf * Nfp + cnt++] = n;
+        int key = D == 2 ? bary(n, corners[1]) : bary(n, corners[2]) * (P + 1) + bary(n, corners[1]);
+        rest.push_back({key, n});
       }
+    std::sort(rest.begin(), rest.end());
+    for (auto& kn : rest) {
+      if (cnt >= Nfp) throw std::runtime_error("too many face nodes");
+      m_locFaceNodes[lf * Nfp + cnt++] = kn.second;
     }
     if (cnt != Nfp) throw std::runtime_error("face node count mismatch");
     for (int m = 0; m < Nfp; ++m) {
