@@ -3,6 +3,13 @@
 #include <exception>
 #include <string>
 
+#include "mshio.h"
+
+// Opaque mesh handle of the C API (include/dgfem_host.h).
+struct dgh_mesh {
+  dgmsh::VolumeMesh m;
+};
+
 namespace dghost {
 void set_error(const std::string& s);
 

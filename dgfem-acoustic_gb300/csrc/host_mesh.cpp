@@ -8,10 +8,6 @@
 #include "host_common.h"
 #include "mshio.h"
 
-struct dgh_mesh {
-  dgmsh::VolumeMesh m;
-};
-
 namespace dghost {
 thread_local std::string g_last_error;
 void set_error(const std::string& s) { g_last_error = s; }

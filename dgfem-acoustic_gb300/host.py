@@ -99,3 +99,147 @@ def schedule(t_start, t_end, dt, t_rate):
     L.dgh_schedule(t_start, t_end, dt, t_rate, times.ctypes.data_as(C.POINTER(C.c_double)),
                    snap.ctypes.data_as(C.POINTER(C.c_ubyte)))
     return times, snap.astype(bool)
+
+
+def _setup_more(L):
+    if getattr(L, "_more", False):
+        return
+    L.dgh_config_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    L.dgh_config_free.argtypes = [C.c_void_p]
+    for fn in ("dgh_config_mesh_file", "dgh_config_time_method", "dgh_config_element_type", "dgh_config_precision"):
+        getattr(L, fn).argtypes = [C.c_void_p]
+        getattr(L, fn).restype = C.c_char_p
+    L.dgh_config_numbers.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 7
+    for fn in ("dgh_config_num_threads", "dgh_config_num_bc", "dgh_config_num_sources", "dgh_config_num_observers",
+               "dgh_config_num_ics"):
+        getattr(L, fn).argtypes = [C.c_void_p]
+    L.dgh_config_bc.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.dgh_config_source.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_char_p), C.POINTER(C.c_int64), C.POINTER(C.POINTER(C.c_double))]
+    L.dgh_config_observer.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    L.dgh_config_ic.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    L.dgh_source_value.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.dgh_source_value.restype = C.c_double
+    L.dgh_formula_eval.argtypes = [C.c_char_p, C.c_double, C.POINTER(C.c_double)]
+    L.dgh_write_pvd.argtypes = [C.c_char_p] + [C.c_double] * 4
+    L.dgh_write_wav.argtypes = [C.c_char_p, C.POINTER(C.c_float), C.c_int64, C.c_uint32]
+    L.dgh_read_wav.argtypes = [C.c_char_p, C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.c_int64),
+                               C.POINTER(C.c_uint32)]
+    L.dgh_free.argtypes = [C.c_void_p]
+    L.dgh_write_spectra.argtypes = [C.c_char_p, C.POINTER(C.c_float), C.c_int64, C.c_double]
+    L.dgh_spectra.argtypes = [C.POINTER(C.c_float), C.c_int64, C.c_double, C.POINTER(C.c_int64),
+                              C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L._more = True
+
+
+def load_config(path, times=None):
+    """Parses a .conf/.json configuration (and its mesh) like the reference.
+    With times, also returns source_values[len(times)][n_sources] (NaN where a
+    source writes nothing)."""
+    L = lib()
+    _setup_more(L)
+    h = C.c_void_p()
+    if L.dgh_config_load(path.encode(), C.byref(h)) != 0:
+        raise RuntimeError(_err())
+    try:
+        nums = [C.c_double() for _ in range(4)]
+        v0 = (C.c_double * 3)()
+        rho0, c0 = C.c_double(), C.c_double()
+        L.dgh_config_numbers(h, *[C.byref(x) for x in nums], v0, C.byref(rho0), C.byref(c0))
+        out = dict(mesh_file=L.dgh_config_mesh_file(h).decode(), time_method=L.dgh_config_time_method(h).decode(),
+                   element_type=L.dgh_config_element_type(h).decode(), precision=L.dgh_config_precision(h).decode(),
+                   t_start=nums[0].value, t_end=nums[1].value, dt=nums[2].value, t_rate=nums[3].value,
+                   v0=tuple(v0), rho0=rho0.value, c0=c0.value, num_threads=L.dgh_config_num_threads(h))
+        bcs = []
+        for i in range(L.dgh_config_num_bc(h)):
+            t, ty = C.c_int(), C.c_int()
+            L.dgh_config_bc(h, i, C.byref(t), C.byref(ty))
+            bcs.append((t.value, ty.value))
+        out["bcs"] = bcs
+        srcs = []
+        for i in range(L.dgh_config_num_sources(h)):
+            kind, params = C.c_int(), (C.c_double * 8)()
+            formula, rows, tab = C.c_char_p(), C.c_int64(), C.POINTER(C.c_double)()
+            L.dgh_config_source(h, i, C.byref(kind), params, C.byref(formula), C.byref(rows), C.byref(tab))
+            table = np.ctypeslib.as_array(tab, shape=(rows.value * 2,)).reshape(-1, 2).copy() if rows.value else None
+            srcs.append(dict(kind=kind.value, params=list(params), formula=formula.value.decode(), table=table))
+        out["sources"] = srcs
+        obs = []
+        for i in range(L.dgh_config_num_observers(h)):
+            v = (C.c_double * 4)()
+            L.dgh_config_observer(h, i, v)
+            obs.append(tuple(v))
+        out["observers"] = obs
+        ics = []
+        for i in range(L.dgh_config_num_ics(h)):
+            v = (C.c_double * 5)()
+            L.dgh_config_ic(h, i, v)
+            ics.append(tuple(v))
+        out["ics"] = ics
+        if times is not None:
+            out["source_values"] = np.array([[L.dgh_source_value(h, i, float(t)) for i in range(len(srcs))]
+                                             for t in times]).reshape(len(times), len(srcs))
+        return out
+    finally:
+        L.dgh_config_free(h)
+
+
+def formula(expr, t):
+    """(ok, value) of the formula evaluator."""
+    L = lib()
+    _setup_more(L)
+    v = C.c_double()
+    rc = L.dgh_formula_eval(expr.encode(), t, C.byref(v))
+    return rc == 0, v.value
+
+
+def write_wav(path, samples, rate):
+    L = lib()
+    _setup_more(L)
+    s = np.ascontiguousarray(samples, dtype=np.float32)
+    if L.dgh_write_wav(path.encode(), s.ctypes.data_as(C.POINTER(C.c_float)), len(s), rate) != 0:
+        raise RuntimeError(_err())
+
+
+def read_wav(path):
+    L = lib()
+    _setup_more(L)
+    p, n, r = C.POINTER(C.c_float)(), C.c_int64(), C.c_uint32()
+    if L.dgh_read_wav(path.encode(), C.byref(p), C.byref(n), C.byref(r)) != 0:
+        raise RuntimeError(_err())
+    out = np.ctypeslib.as_array(p, shape=(max(n.value, 1),))[:n.value].copy()
+    L.dgh_free(p)
+    return out, r.value
+
+
+def spectra(p, dt):
+    """(fft rows [nb/2,5], psd rows [nb/2+1,3]) of a pressure trace."""
+    L = lib()
+    _setup_more(L)
+    s = np.ascontiguousarray(p, dtype=np.float32)
+    nb = 1
+    while nb * 2 <= len(s):
+        nb *= 2
+    f = np.zeros((nb // 2 + 1, 5))
+    q = np.zeros((nb // 2 + 2, 3))
+    nbo = C.c_int64()
+    if L.dgh_spectra(s.ctypes.data_as(C.POINTER(C.c_float)), len(s), dt, C.byref(nbo),
+                     f.ctypes.data_as(C.POINTER(C.c_double)), q.ctypes.data_as(C.POINTER(C.c_double))) != 0:
+        raise RuntimeError(_err())
+    n = nbo.value
+    return f[:n // 2], q[:n // 2 + 1]
+
+
+def write_spectra(prefix, p, dt):
+    L = lib()
+    _setup_more(L)
+    s = np.ascontiguousarray(p, dtype=np.float32)
+    if L.dgh_write_spectra(prefix.encode(), s.ctypes.data_as(C.POINTER(C.c_float)), len(s), dt) != 0:
+        raise RuntimeError(_err())
+
+
+def write_pvd(path, t_start, t_end, dt, t_rate):
+    L = lib()
+    _setup_more(L)
+    if L.dgh_write_pvd(path.encode(), t_start, t_end, dt, t_rate) != 0:
+        raise RuntimeError(_err())

@@ -53,6 +53,9 @@ void dgh_config_free(dgh_config* c);
 const char* dgh_config_mesh_file(const dgh_config* c);
 const char* dgh_config_time_method(const dgh_config* c);
 const char* dgh_config_element_type(const dgh_config* c);
+/* project extension: working precision "fp64" (default) or "fp32"
+ * (.json: "gpu": {"precision": ...}; .conf: gpuPrecision = ...) */
+const char* dgh_config_precision(const dgh_config* c);
 /* t_start, t_end, dt, t_rate, v0[3], rho0, c0 */
 void dgh_config_numbers(const dgh_config* c, double* t_start, double* t_end, double* dt, double* t_rate,
                         double* v0, double* rho0, double* c0);

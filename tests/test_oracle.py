@@ -1,0 +1,110 @@
+"""The CPU oracle: exactness of its basis/quadrature on linear fields, the
+penalty-sign recipe, the time schedule, and the pin against the reference's
+golden residual trace (cases/2d_hilltop, residuals.csv)."""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def _mesh(pkg, dim, p, n=3):
+    mg = pkg.meshgen
+    m = mg.square(n=n, order=p, seed=7) if dim == 2 else mg.box(counts=(n, n, n), order=p, seed=8)
+    return dict(dim=dim, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"], groups=[])
+
+
+@pytest.mark.parametrize("dim,p", [(2, 1), (2, 2), (2, 3), (2, 4), (3, 1), (3, 2), (3, 3)])
+def test_linear_fields_give_exact_derivatives(pkg, oracle, dim, p):
+    """On interior elements dv/dt = -grad p / rho0 and dp/dt = -rho0 c0^2 div v."""
+    mesh = _mesh(pkg, dim, p)
+    rho0, c0 = 1.3, 2.0
+    P = oracle.Problem(mesh, rho0=rho0, c0=c0, dt=1.0)
+    x = mesh["xyz"][mesh["elem_nodes"].reshape(-1)]
+    interior = (P.faces()["nbr"] >= 0).all(axis=1)
+    npe = mesh["elem_nodes"].shape[1]
+    u = np.zeros((4, x.shape[0]))
+    u[0] = 2.0 * x[:, 0] - 3.0 * x[:, 1]
+    k = P.stage(u).reshape(4, -1, npe)
+    np.testing.assert_allclose(k[1][interior], -2.0 / rho0, rtol=1e-10)
+    np.testing.assert_allclose(k[2][interior], 3.0 / rho0, rtol=1e-10)
+    u = np.zeros((4, x.shape[0]))
+    u[1] = x[:, 0]
+    u[2] = 2 * x[:, 1]
+    k = P.stage(u).reshape(4, -1, npe)
+    np.testing.assert_allclose(k[0][interior], -3.0 * rho0 * c0 ** 2, rtol=1e-10)
+
+
+@pytest.mark.parametrize("dim,p", [(2, 1), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4)])
+def test_penalty_sign_recipe_is_dissipative(pkg, oracle, dim, p):
+    """The reference's LF penalty sign fc * orientation(up) (Mesh.cpp:366-367,
+    :452-477, :792) must be +1 on every interior face of positively oriented
+    meshes with the oracle's face quadrature (fc = -1 for 3-D p != 1 is
+    compensated by the reversed recipe normal)."""
+    mesh = _mesh(pkg, dim, p, n=2)
+    f = oracle.Problem(mesh, dt=1.0).faces()
+    assert np.all(f["penalty"][f["nbr"] >= 0] == 1)
+
+
+def test_schedule_matches_reference_loop(oracle):
+    P = oracle.Problem(dict(dim=2, order=1, xyz=np.zeros((3, 3)), elem_nodes=np.array([[0, 1, 2]]), groups=[]),
+                       t_start=0.0, t_end=1.0, dt=1e-3, t_rate=0.1)
+    assert P.count_steps() == (1000, 10)
+
+
+def _hilltop(pkg, oracle, max_steps=-1, threads=1):
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "m.msh")
+        with gzip.open(os.path.join(GOLDEN, "2d_hilltop_fs.msh.gz"), "rb") as f:
+            open(path, "wb").write(f.read())
+        m = pkg.host.load_mesh(path)
+    assert [g[1] for g in m["groups"]] == ["abs", "ref"]
+    mesh = dict(dim=2, order=1, xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                groups=[(0, m["groups"][0][2]), (1, m["groups"][1][2])])
+    P = oracle.Problem(mesh, rho0=1.225, c0=340.0, t_end=1.0, dt=1e-3, t_rate=0.1, observers=[(500, 2, 0, 10)],
+                       ics=[(0, 200, 0, 2000, 1.0)], max_steps=max_steps, num_threads=threads)
+    return P.run()
+
+
+def test_oracle_matches_reference_golden_trace(pkg, oracle):
+    """Rows dominated by the physical change (the last 40 steps of every 0.1 s
+    snapshot interval) agree with the reference run; rows right after a
+    snapshot measure a one-step change, where the reference run's data race
+    in the nested face loop (Mesh.cpp:764-808, 20 threads) dominates."""
+    r = _hilltop(pkg, oracle)
+    gold = np.genfromtxt(os.path.join(GOLDEN, "hilltop_residuals.csv"), delimiter=";", skip_header=1)
+    assert r["steps"] == gold.shape[0] == 1000
+    assert list(r["snapshots"]) == list(range(0, 1000, 100))
+    np.testing.assert_allclose(r["times"], gold[:, 0], atol=1e-9)
+    for k in range(10):
+        rows = np.arange(100 * k + 60, 100 * k + 100)
+        rel = np.abs(r["residuals"][rows, :4] - gold[rows, 1:5]) / gold[rows, 1:5]
+        assert rel.max() < (0.05 if k < 1 else 0.1), (k, rel.max(axis=0))
+    # interval 1 (t in [0.16, 0.2)) pins the pressure residual to 0.4 %
+    rows = np.arange(160, 200)
+    assert np.max(np.abs(r["residuals"][rows, 0] - gold[rows, 1]) / gold[rows, 1]) < 4e-3
+    assert np.all(r["residuals"][:, 4] == 0.0)
+    assert r["penalty_hist"][0] == 0
+
+
+def test_golden_trace_discriminates(pkg, oracle):
+    """A wrong physical parameter (c0 off by 2 %) is caught by the same rows."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "m.msh")
+        with gzip.open(os.path.join(GOLDEN, "2d_hilltop_fs.msh.gz"), "rb") as f:
+            open(path, "wb").write(f.read())
+        m = pkg.host.load_mesh(path)
+    mesh = dict(dim=2, order=1, xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                groups=[(0, m["groups"][0][2]), (1, m["groups"][1][2])])
+    P = oracle.Problem(mesh, rho0=1.225, c0=340.0 * 1.02, t_end=1.0, dt=1e-3, t_rate=0.1,
+                       ics=[(0, 200, 0, 2000, 1.0)], max_steps=200)
+    r = P.run()
+    gold = np.genfromtxt(os.path.join(GOLDEN, "hilltop_residuals.csv"), delimiter=";", skip_header=1)
+    rows = np.arange(160, 200)
+    assert np.max(np.abs(r["residuals"][rows, 0] - gold[rows, 1]) / gold[rows, 1]) > 1e-2
