@@ -1,0 +1,304 @@
+"""Benchmark: RK4 DOF-updates/s of the GB300 DG solver on the 3-D LEE
+workload (cube [-1,1]^3, 32^3 x 6 = 196,608 jittered tetrahedra, p = 3,
+quiescent medium rho0 = 1.225, c0 = 340, 50 Hz monopole at the centre,
+Reflecting on x = +-1, Absorbing elsewhere, dt from CFL 0.5, 8 observers).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
+  python bench.py --impl reference ...   (the reference's CPU path, restated)
+
+One step = one full RK4 time step of the reference's loop (source injection,
+four RHS stages, the combine, the residual diagnostic and the observer
+samples) over the whole mesh. Prints one JSON line (rank 0).
+
+Multi-GPU runs are independent replicas (one solver per GPU, no collective
+on the data path); value = DOF-updates of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="3D LEE cube, 196,608 tets, p=3", counts=(32, 32, 32), order=3, jitter=0.2, seed=2,
+                rho0=1.225, c0=340.0, v0=(0.0, 0.0, 0.0), freq=50.0, amp=0.1, size=0.1, cfl=0.5, n_obs=8)
+BCS = {"xmin": "Reflecting", "xmax": "Reflecting", "ymin": "Absorbing", "ymax": "Absorbing", "zmin": "Absorbing",
+       "zmax": "Absorbing"}
+METRIC = "RK4 DOF-updates/s"
+UNIT = "DOF-updates/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _pkg():
+    import importlib
+    return importlib.import_module("dgfem-acoustic_gb300")
+
+
+def _oracle():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("refcpu", os.path.join(ROOT, "oracle", "refcpu.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def build_problem(counts=None):
+    """Mesh, solver groups, dt, sources and observers of the workload."""
+    pkg = _pkg()
+    W = WORKLOAD
+    m = pkg.meshgen.box(counts=counts or W["counts"], order=W["order"], jitter=W["jitter"], seed=W["seed"])
+    mesh = dict(dim=3, order=W["order"], xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                groups=pkg.meshgen.solver_groups(m, BCS))
+    # dt = CFL * h_min / ((c0 + |v0|) (2p + 1)), h_min = shortest element edge
+    en, X = m["elem_nodes"][:, :4], m["xyz"]
+    hmin = min(np.linalg.norm(X[en[:, a]] - X[en[:, b]], axis=1).min() for a in range(4) for b in range(a + 1, 4))
+    dt = W["cfl"] * hmin / ((W["c0"] + np.linalg.norm(W["v0"])) * (2 * W["order"] + 1))
+    rng = np.random.default_rng(W["seed"])
+    obs = [tuple(rng.uniform(-0.8, 0.8, 3)) + (0.1,) for _ in range(W["n_obs"])]
+    src = [0.0, 0.0, 0.0, W["size"], W["amp"], W["freq"], 0.0, 1e9]
+    return mesh, dt, src, obs
+
+
+def node_sets(mesh, src, obs):
+    x = mesh["xyz"][mesh["elem_nodes"].reshape(-1)]
+    d2 = (x[:, 0] - src[0]) ** 2 + (x[:, 1] - src[1]) ** 2 + (x[:, 2] - src[2]) ** 2
+    sdofs = [np.nonzero(d2 < src[3] ** 2)[0]]
+    odofs, ows = [], []
+    for o in obs:
+        d = np.sqrt((x[:, 0] - o[0]) ** 2 + (x[:, 1] - o[1]) ** 2 + (x[:, 2] - o[2]) ** 2)
+        idx = np.nonzero(d < o[3])[0]
+        odofs.append(idx)
+        ows.append(1.0 / (d[idx] ** 2 + 1e-12))
+    return sdofs, odofs, ows
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) > 8 for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the stage kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "stage_kernel_traffic.json")
+    try:
+        d = json.load(open(p))
+        return d.get("bytes_per_launch_full_workload")
+    except Exception:
+        return None
+
+
+def run_gpu(args, rank, world):
+    pkg = _pkg()
+    import ctypes
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    mesh, dt, src, obs = build_problem()
+    prec = pkg.gpu.DG_FP32 if args.precision == "fp32" else pkg.gpu.DG_FP64
+    W = WORKLOAD
+    S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=prec, device=device)
+    info = S.info()
+    E, np_ = mesh["elem_nodes"].shape
+    nv = 4
+    dofs = E * np_ * nv
+    sdofs, odofs, ows = node_sets(mesh, src, obs)
+    S.set_sources(sdofs)
+    nsteps_total = args.warmup + 3 * args.steps + 8
+    times = np.arange(nsteps_total) * dt
+    S.set_source_values((src[4] * np.sin(2 * np.pi * src[5] * times + src[6]))[:, None])
+    S.set_observers(odofs, ows)
+    u0 = np.zeros((4, E * np_))
+    S.set_state(u0)
+    S.snapshot()
+    # warm-up (also builds the per-step graph)
+    S.run(args.warmup, dt)
+    barrier(world)
+    # ---- timed device region: per-step CUDA events on the solver's stream ----
+    with ClockSampler(device) as clk:
+        step_ms, kern_ms = S.bench_steps(args.steps, dt, flush_bytes=L2_FLUSH_BYTES, kernel_time=True)
+    total_ms = step_ms * args.steps
+    total_ms = allmax(total_ms, world)
+    # ---- end-to-end through the C ABI with host buffers ----
+    u_host = np.zeros((4, E * np_))
+    barrier(world)
+    t0 = time.perf_counter()
+    S.set_state(u_host)
+    res, tr = S.run(args.steps, dt)
+    u_out = S.get_state()
+    e2e_s = time.perf_counter() - t0
+    e2e_s = allmax(e2e_s, world)
+    state_bytes = 4 * E * np_ * 8
+    h2d = state_bytes / args.steps + 8 * 1
+    d2h = state_bytes / args.steps + 5 * 8 + len(obs) * 4 * 8
+    # roofline of the stage kernel: algorithmic bytes of one RK4 step's four
+    # launches (18 state words per DOF incl. the residual snapshot read, plus
+    # the per-element geometry records read once per stage) / their time
+    w = 4 if args.precision == "fp32" else 8
+    recf = 28 if args.precision == "fp32" else 26
+    geo_bytes = 4 * E * (recf * w + 8 * 4)
+    alg_bytes = 18 * dofs * w + geo_bytes
+    peak, peak_kind = measured_peak_gbs()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    value = world * dofs * args.steps / (total_ms * 1e-3)
+    e2e_value = world * dofs * args.steps / e2e_s
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic (seeded jittered mesh, monopole)",
+        "config": {"workload": WORKLOAD["name"], "elements": int(E), "order": 3, "n_var": nv, "dofs": int(dofs),
+                   "dt": dt, "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "step": "source inject + 4 fused RK4 stages + residual + 8 observers (one CUDA graph)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "note": "dg_set_state + dg_run(K steps, host residual/observer arrays) + dg_get_state"},
+        "gpu_launches": int(args.steps * 8),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "stage_kernel (4 launches per step)",
+                     "kernel_ms_per_step": kern_ms, "algorithmic_bytes_per_step": int(alg_bytes)},
+        "clocks": clk.summary(),
+        "setup_ms": info["setup_ms"],
+    }
+    S.close()
+    return line
+
+
+def run_cpu_baseline(args, sample_counts=(12, 12, 12), steps=4):
+    """The oracle in the reference's loop structure and pragmas, all host
+    threads, on a bounded sample of the workload (same order and physics,
+    a 12^3 x 6 = 10,368-tet box)."""
+    oracle = _oracle()
+    W = WORKLOAD
+    mesh, dt, src, obs = build_problem(sample_counts)
+    cores = os.cpu_count() or 1
+    P = oracle.Problem(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], t_start=0.0, t_end=1.0, dt=dt, t_rate=1.0,
+                       num_threads=cores, sources=[dict(kind=oracle.SRC_SINE, params=src)], observers=obs,
+                       max_steps=steps)
+    r = P.run()
+    E, np_ = mesh["elem_nodes"].shape
+    rate = E * np_ * 4 * r["steps"] / r["loop_seconds"]
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d steps on a %dx%dx%d x 6 = %d-tet box of the same workload (p=3, same physics), "
+                      "reference loop structure and OpenMP pragmas, setup %.1f s excluded"
+                      % (r["steps"], *sample_counts, E, r["setup_seconds"])}
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        if rank == 0:
+            # each "step" of this arm is one reference time step on the bounded sample
+            t0 = time.perf_counter()
+            base = run_cpu_baseline(args, steps=max(1, min(args.steps, 6)))
+            line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "f64", "data": "synthetic (seeded jittered mesh, monopole)", "impl": "reference",
+                    "config": {"workload": WORKLOAD["name"], "parallelism": "host threads (OpenMP)"},
+                    "cpu_baseline": base,
+                    "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    "wall_s": time.perf_counter() - t0}
+            print(json.dumps(line), flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    # the oracle is timed before any CUDA call (its OpenMP team must not be
+    # forked after the GPU is initialised)
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        base = run_cpu_baseline(args)
+    line = run_gpu(args, rank, world)
+    if rank == 0:
+        line["cpu_baseline"] = base
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
