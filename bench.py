@@ -216,6 +216,27 @@ def run_gpu(args, rank, world):
     return line
 
 
+def run_profile(args):
+    """Warm-up plus a few RK4 steps of the workload through the per-step graph,
+    nothing else (the command line that the ncu summaries in profiles/ use)."""
+    pkg = _pkg()
+    mesh, dt, src, obs = build_problem()
+    W = WORKLOAD
+    prec = pkg.gpu.DG_FP32 if args.precision == "fp32" else pkg.gpu.DG_FP64
+    S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=prec, device=0)
+    sdofs, odofs, ows = node_sets(mesh, src, obs)
+    S.set_sources(sdofs)
+    n = args.warmup + args.steps
+    times = np.arange(n) * dt
+    S.set_source_values((src[4] * np.sin(2 * np.pi * src[5] * times + src[6]))[:, None])
+    S.set_observers(odofs, ows)
+    S.snapshot()
+    S.run(args.warmup, dt)
+    res, _ = S.run(args.steps, dt)
+    print(json.dumps({"profile": True, "steps": args.steps, "warmup": args.warmup, "res_p_last": float(res[-1, 0])}))
+    S.close()
+
+
 def run_cpu_baseline(args, sample_counts=(12, 12, 12), steps=4):
     """The oracle in the reference's loop structure and pragmas, all host
     threads, on a bounded sample of the workload (same order and physics,
@@ -260,6 +281,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="only build the workload and run warmup + steps time steps (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -267,6 +290,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         if rank == 0:
             # each "step" of this arm is one reference time step on the bounded sample
