@@ -4,6 +4,7 @@
 // reductions) and benchmarking.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -205,11 +206,19 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   a.fmask = c->fmask;
   a.nbrnode = c->nbrnode;
   a.stride = c->Epad * c->np;
-  a.ntiles = (int)c->ntiles;
+  a.ntiles = c->variant >= 0 ? (int)(c->Epad / c->s2.et) : (int)c->ntiles;
   a.stage = stage;
   a.dt = dt;
   a.c0sq = c->c0sq;
   a.ph = c->ph;
+  if (c->variant >= 0) {
+    if constexpr (sizeof(T) == 4)
+      return c->dim == 2 ? dgk::launch_stage2_f32_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+                         : dgk::launch_stage2_f32_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
+    else
+      return c->dim == 2 ? dgk::launch_stage2_f64_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+                         : dgk::launch_stage2_f64_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
+  }
   if constexpr (sizeof(T) == 4)
     return c->dim == 2 ? dgk::launch_stage_f32_2d(c->order, a, c->grid, c->stream)
                        : dgk::launch_stage_f32_3d(c->order, a, c->grid, c->stream);
@@ -239,7 +248,7 @@ cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
           c->n_src_dofs);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
-  int nparts = c->grid;
+  int nparts = c->variant >= 0 ? c->grid2 : c->grid;
   if (kind == 0) {
     const void* in[4] = {c->u, c->y0, c->y1, c->y0};
     void* out[4] = {c->y0, c->y1, c->y0, nullptr};
@@ -329,9 +338,12 @@ int run_steps(dg_ctx* c, int kind, int64_t n_steps, double dt, double* residuals
   CK(c, cudaMemcpyAsync(res.data(), c->d_res, n_steps * 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (obs && c->n_obs > 0)
     CK(c, cudaMemcpyAsync(obs, c->d_obs, n_steps * c->n_obs * 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  int herr = 0;
+  CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->step += n_steps;
   if (residuals) std::memcpy(residuals, res.data(), res.size() * sizeof(double));
+  if (herr) return fail(c, DG_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy did not complete)");
   for (double v : res)
     if (!std::isfinite(v)) return fail(c, DG_ERR_NONFINITE, "non-finite values in the state (residual is NaN/Inf)");
   return DG_OK;
@@ -347,6 +359,77 @@ void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>&
   L.resize(nk * np);
   for (int k = 0; k < nk; ++k)
     for (int i = 0; i < np; ++i) L[k * np + i] = (T)re.LIFT[i * nk + k];
+}
+
+
+dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
+  if (c->prec == DG_FP32) return c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v) : dgk::stage2_info_f32_3d(c->order, v);
+  return c->dim == 2 ? dgk::stage2_info_f64_2d(c->order, v) : dgk::stage2_info_f64_3d(c->order, v);
+}
+
+// Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k.
+bool set_variant(dg_ctx* c, int v) {
+  if (v < 0) {
+    c->variant = -1;
+    return true;
+  }
+  dgk::Stage2Info si = stage2_info(c, v);
+  if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return false;
+  c->variant = v;
+  c->s2 = si;
+  c->grid2 = (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms);
+  if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
+  return true;
+}
+
+// Autotuner: times one RK stage (stage 2: reads y, u, acc; writes acc, y) of
+// every kernel variant on this mesh and keeps the fastest. want >= -1 forces
+// a variant instead.
+int select_variant(dg_ctx* c, int want) {
+  if (want >= -1) {
+    if (!set_variant(c, want)) return fail(c, DG_ERR_ARG, "stage kernel variant not available");
+    return DG_OK;
+  }
+  std::vector<int> cands{-1};
+  for (int v = 0; v < 8; ++v) {
+    dgk::Stage2Info si = stage2_info(c, v);
+    if (si.nc == 0) break;
+    if (si.blocks_per_sm > 0) cands.push_back(v);
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int best_v = -1;
+  for (int v : cands) {
+    if (!set_variant(c, v)) continue;
+    cudaError_t err = cudaSuccess;
+    for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = launch_stage(c, 2, c->y0, c->y1, nullptr, 1e-30);
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < 4 && err == cudaSuccess; ++r) err = launch_stage(c, 2, c->y0, c->y1, nullptr, 1e-30);
+    cudaEventRecord(e1, c->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+    if (err != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(c, DG_ERR_CUDA, std::string("CUDA (autotune): ") + cudaGetErrorString(err));
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms, best_v = v;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int zero = 0;
+  cudaMemcpy(c->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+  // the timing runs wrote the accumulator and stage buffers only; clear them
+  const size_t nb = (size_t)c->nv * c->Epad * c->np * c->tsize;
+  cudaMemsetAsync(c->acc, 0, nb, c->stream);
+  cudaMemsetAsync(c->y0, 0, nb, c->stream);
+  cudaMemsetAsync(c->y1, 0, nb, c->stream);
+  cudaStreamSynchronize(c->stream);
+  set_variant(c, best_v);
+  return DG_OK;
 }
 
 }  // namespace
@@ -397,8 +480,8 @@ int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int 
     return bad(DG_ERR_ARG, "nodes_per_elem does not match dim/order");
   }
   c->E = mesh->n_elems, c->nnodes = mesh->n_nodes;
-  c->ntiles = (c->E + c->sh.et - 1) / c->sh.et;
-  c->Epad = c->ntiles * c->sh.et;
+  c->Epad = (c->E + dgk::kElemAlign - 1) / dgk::kElemAlign * dgk::kElemAlign;
+  c->ntiles = c->Epad / c->sh.et;
   if (c->Epad >= (int64_t)1 << 31) {
     delete c;
     return bad(DG_ERR_ARG, "too many elements");
@@ -516,7 +599,15 @@ int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int 
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_perm, c->np * sizeof(int));
   if (e == cudaSuccess) e = cudaMemcpy(c->d_perm, c->perm_c2i.data(), c->np * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_ref, 4 * c->E * c->np * sizeof(double));
-  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->partials, std::max(c->grid, 2 * c->num_sms) * 5 * sizeof(double));
+  c->max_grid = std::max(c->grid, 2 * c->num_sms);
+  for (int v = 0; v < 8; ++v) {
+    dgk::Stage2Info si = stage2_info(c, v);
+    if (si.nc == 0) break;
+    c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
+  }
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->partials, c->max_grid * 5 * sizeof(double));
+  if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_step, 2 * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_step, 0, 2 * sizeof(int64_t), c->stream);
   cudaEventRecord(t1, c->stream);
@@ -537,6 +628,17 @@ int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int 
   c->info.n_boundary_faces = c->n_bfaces;
   c->info.device_bytes = c->device_bytes;
   c->info.setup_ms = ms;
+  {
+    const char* ev = std::getenv("DGFEM_STAGE_VARIANT");
+    int want = ev ? std::atoi(ev) : -2;
+    int rc2 = select_variant(c, want);
+    if (rc2 != DG_OK) {
+      std::string m = c->err;
+      dg_destroy(c);
+      return bad(rc2, m);
+    }
+  }
+  c->info.kernel_variant = c->variant;
   *out = c;
   return DG_OK;
 }
@@ -762,6 +864,13 @@ int dg_face_info(dg_ctx* c, int64_t* nbr, int* penalty, int* bc) {
 }
 
 void* dg_stream(dg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int dg_tune(dg_ctx* c, int variant) {
+  if (!c) return DG_ERR_ARG;
+  int rc = select_variant(c, variant);
+  c->info.kernel_variant = c->variant;
+  return rc;
+}
 
 int dg_bench_steps(dg_ctx* c, int64_t n_steps, double dt, int64_t flush_bytes, double* step_ms, double* kernel_ms) {
   if (!c || n_steps <= 0 || !(dt > 0)) return DG_ERR_ARG;

@@ -24,6 +24,10 @@ struct dg_ctx {
   // device
   cudaStream_t stream = nullptr;
   int num_sms = 0, grid = 0;
+  // stage kernel selection: -1 = baseline kernel (stage.cuh), k >= 0 = pipelined variant k (stage2.cuh)
+  int variant = -1, grid2 = 0, max_grid = 0;
+  dgk::Stage2Info s2{};
+  int* d_err = nullptr;  // device error flags of bounded waits
   size_t tsize = 8;
   void* u = nullptr;     // state            [nv][Epad*np]
   void* acc = nullptr;   // RK accumulator

@@ -89,6 +89,22 @@ int blocks_per_sm_f32_3d(int order);
 int blocks_per_sm_f64_2d(int order);
 int blocks_per_sm_f64_3d(int order);
 
+// Pipelined stage kernel (stage2.cuh): variants differ in nodes per thread
+// and elements per tile; the context picks one by timing (autotuning).
+struct Stage2Info {
+  int nc, et, nt, smem_bytes, blocks_per_sm, n_variants;
+};
+cudaError_t launch_stage2_f32_2d(int order, int variant, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
+cudaError_t launch_stage2_f32_3d(int order, int variant, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
+cudaError_t launch_stage2_f64_2d(int order, int variant, const StageArgs<double>& a, int grid, int* err, cudaStream_t s);
+cudaError_t launch_stage2_f64_3d(int order, int variant, const StageArgs<double>& a, int grid, int* err, cudaStream_t s);
+Stage2Info stage2_info_f32_2d(int order, int variant);
+Stage2Info stage2_info_f32_3d(int order, int variant);
+Stage2Info stage2_info_f64_2d(int order, int variant);
+Stage2Info stage2_info_f64_3d(int order, int variant);
+// element padding: every tile size divides this
+constexpr int kElemAlign = 128;
+
 // Host-side shape queries for a runtime (dim, order).
 struct ShapeInfo {
   int np, nf, nfp, nv, nperm, et, nt, recf32, recf64, reci;

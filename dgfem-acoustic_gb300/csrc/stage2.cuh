@@ -1,0 +1,441 @@
+// Pipelined fused RK4 stage kernel (sm_103a).
+//
+// Same arithmetic as the reference's per-stage work (src/Mesh.cpp:734-975,
+// src/solver.cpp:38-57, :488-516), organised for memory-level parallelism:
+//
+//   persistent blocks, one tile of ET consecutive elements at a time;
+//   * the tile's stage input and geometry records arrive by TMA bulk copies
+//     (cp.async.bulk, mbarrier completion) into a double buffer: the next
+//     tile is in flight while the current one computes;
+//   * the tile's RK operands (u, accumulator, residual snapshot) arrive by a
+//     second TMA group issued at tile start and consumed by the epilogue;
+//   * neighbour traces are gathered with per-thread cp.async (LDGSTS) issued
+//     before the volume contraction and awaited after it;
+//   * volume contraction W^r = Dt_r y (shared operators, register blocked:
+//     each thread owns NC output nodes of one element), flux mixing, face
+//     numerical fluxes, LIFT, and the RK update straight from registers with
+//     vectorised coalesced stores.
+// Every mbarrier wait is bounded; on timeout the block records an error flag
+// and finishes its loop without further waiting.
+#pragma once
+#include <cstdint>
+
+#include "dg_internal.cuh"
+
+namespace dgk {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 1-D TMA bulk copy global -> shared, completion counted on bar (bytes % 16 == 0,
+// both addresses 16-byte aligned).
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (int it = 0; it < (1 << 20); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait_all() {
+  asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int N, int A>
+struct RoundUp {
+  static constexpr int v = (N + A - 1) / A * A;
+};
+
+// Compile-time configuration: element shape (D, P), precision T, nodes per
+// thread NC and elements per tile ET.
+template <typename T, int D, int P, int NC_, int ET_>
+struct Pipe {
+  using S = ShapeT<D, P, T>;
+  static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NV = S::NV, NPERM = S::NPERM, NK = NF * NFP;
+  static constexpr int NC = NC_;
+  static constexpr int NSPLIT = (NP + NC - 1) / NC;
+  static constexpr int ET = ET_;
+  static constexpr int NT = ET * NSPLIT;
+  static constexpr int RECF = S::RECF, RECI = S::RECI;
+  static constexpr int Q4 = 4;  // variables per face node slot (vz slot unused in 2-D)
+  // byte sizes of the TMA segments
+  static constexpr uint32_t YSEG = ET * NP * sizeof(T);  // one variable of the tile
+  static constexpr uint32_t GFB = ET * RECF * sizeof(T);
+  static constexpr uint32_t GIB = ET * RECI * sizeof(int);
+  // shared memory layout (bytes)
+  static constexpr size_t oBar = 0;                                        // 3 mbarriers
+  static constexpr size_t oD = 64;                                          // Dt [D][NP j][NP i]
+  static constexpr size_t oL = RoundUp<oD + D * NP * NP * sizeof(T), 16>::v;  // LIFT [NK][NP]
+  static constexpr size_t oFm = RoundUp<oL + NK * NP * sizeof(T), 16>::v;     // fmask
+  static constexpr size_t oNb = oFm + RoundUp<NK * 2, 16>::v;                 // nbrnode
+  static constexpr size_t oY = RoundUp<oNb + NF * NPERM * NFP * 2, 128>::v;   // 2 x [NV][ET][NP]
+  static constexpr size_t oGF = oY + 2 * (size_t)NV * YSEG;                  // 2 x [ET][RECF]
+  static constexpr size_t oGI = oGF + 2 * (size_t)GFB;                        // 2 x [ET][RECI]
+  static constexpr size_t oE = RoundUp<oGI + 2 * (size_t)GIB, 128>::v;       // [3][NV][ET][NP]
+  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                    // [ET][NK][4]
+  static constexpr size_t oR = RoundUp<oN + (size_t)ET * NK * Q4 * sizeof(T), 16>::v;  // [NT/32][5] double
+  static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
+  static_assert(NT % 32 == 0, "threads per block must be a multiple of 32");
+  static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
+};
+
+template <typename T, int D, int P, int NC_, int ET_>
+__global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(const StageArgs<T> a, int* err) {
+  using C = Pipe<T, D, P, NC_, ET_>;
+  constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
+  constexpr int NC = C::NC, NSPLIT = C::NSPLIT, ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::oBar);  // [0],[1]: tile buffers, [2]: epilogue operands
+  T* sD = reinterpret_cast<T*>(sm + C::oD);
+  T* sL = reinterpret_cast<T*>(sm + C::oL);
+  short* sFm = reinterpret_cast<short*>(sm + C::oFm);
+  short* sNb = reinterpret_cast<short*>(sm + C::oNb);
+  T* sYb = reinterpret_cast<T*>(sm + C::oY);
+  T* sGFb = reinterpret_cast<T*>(sm + C::oGF);
+  int* sGIb = reinterpret_cast<int*>(sm + C::oGI);
+  T* sE = reinterpret_cast<T*>(sm + C::oE);
+  T* sN = reinterpret_cast<T*>(sm + C::oN);
+  double* sRed = reinterpret_cast<double*>(sm + C::oR);
+
+  const int tid = threadIdx.x;
+  const int stage = a.stage;
+  const int64_t stride = a.stride;
+  // epilogue operands: stage 1 reads u through the stage input, 2-3 need u and
+  // acc, 4 needs u, acc and the snapshot, 5 (Euler) reads u as the input.
+  const int nepi = (stage == 2 || stage == 3) ? 2 : (stage == 4 ? 3 : 0);
+  const T* epi_src[3] = {a.u, a.acc, a.snap};
+
+  auto issue_tile = [&](int tile, int b) {
+    const int64_t e0 = (int64_t)tile * ET;
+    mbar_expect_tx(&bar[b], NV * C::YSEG + C::GFB + C::GIB);
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      tma_load_1d(sYb + ((size_t)b * NV + q) * ET * NP, a.y_in + q * stride + e0 * NP, C::YSEG, &bar[b]);
+    tma_load_1d(sGFb + (size_t)b * ET * RECF, a.geoF + e0 * RECF, C::GFB, &bar[b]);
+    tma_load_1d(sGIb + (size_t)b * ET * RECI, a.geoI + e0 * RECI, C::GIB, &bar[b]);
+  };
+  auto issue_epi = [&](int tile) {
+    const int64_t e0 = (int64_t)tile * ET;
+    mbar_expect_tx(&bar[2], nepi * NV * C::YSEG);
+    for (int k = 0; k < nepi; ++k)
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+        tma_load_1d(sE + ((size_t)k * NV + q) * ET * NP, epi_src[k] + q * stride + e0 * NP, C::YSEG, &bar[2]);
+  };
+
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    fence_mbar_init();
+  }
+  for (int i = tid; i < D * NP * NP; i += NT) sD[i] = a.Dt[i];
+  for (int i = tid; i < NK * NP; i += NT) sL[i] = a.LIFT[i];
+  for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
+  for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
+  __syncthreads();
+  if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0);
+
+  const T v0x = (T)a.ph.v0[0], v0y = (T)a.ph.v0[1], v0z = (T)a.ph.v0[2];
+  const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
+  const T dt = (T)a.dt;
+  double red[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  bool ok = true;
+  const int e = tid / NSPLIT, s = tid - (tid / NSPLIT) * NSPLIT;
+  const int i0 = s * NC;
+
+  int it = 0;
+  for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    const int64_t e0 = (int64_t)tile * ET;
+    if (ok && !mbar_wait(&bar[b], (it >> 1) & 1)) ok = false;
+    T* sY = sYb + (size_t)b * NV * ET * NP;
+    const T* sGF = sGFb + (size_t)b * ET * RECF;
+    const int* sGI = sGIb + (size_t)b * ET * RECI;
+    if (tid == 0) {
+      fence_proxy_async();
+      const int nt = tile + gridDim.x;
+      if (nt < a.ntiles) issue_tile(nt, b ^ 1);
+      if (nepi > 0) issue_epi(tile);
+    }
+    // ---- neighbour traces: asynchronous gathers into sN ----
+    for (int q8 = tid; q8 < ET * NK; q8 += NT) {
+      const int el = q8 / NK, k = q8 - el * NK;
+      const int f = k / NFP, m = k - f * NFP;
+      const int code = sGI[el * RECI + NF + f];
+      if (!(code & kCodeBoundary)) {
+        const int nbr = sGI[el * RECI + f];
+        const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
+        const T* src = a.y_in + (int64_t)nbr * NP + nn;
+        T* dst = sN + ((size_t)el * NK + k) * C::Q4;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          if (sizeof(T) == 4)
+            cp_async4(dst + q, src + q * stride);
+          else
+            cp_async8(dst + q, src + q * stride);
+        }
+      }
+    }
+    cp_async_commit();
+
+    // ---- volume term for this thread's nodes ----
+    T Lv[NC][NV];
+    {
+      T W[D][NC][NV];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) W[r][ii][q] = 0;
+      const T* ye = sY + e * NP;
+#pragma unroll 4
+      for (int j = 0; j < NP; ++j) {
+        T yq[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          const T* drow = sD + (r * NP + j) * NP;
+#pragma unroll
+          for (int ii = 0; ii < NC; ++ii) {
+            const int i = (i0 + ii < NP) ? i0 + ii : NP - 1;
+            const T dv = drow[i];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) W[r][ii][q] += dv * yq[q];
+          }
+        }
+      }
+      const T* G = sGF + e * RECF;
+      T g[D][D];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[r][d] = G[r * D + d];
+      T gv0[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        gv0[r] = g[r][0] * v0x + g[r][1] * v0y;
+        if (D == 3) gv0[r] += g[r][2] * v0z;
+      }
+#pragma unroll
+      for (int ii = 0; ii < NC; ++ii) {
+        T vp = 0, vv[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) vv[d] = 0;
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          T gw = 0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) gw += g[r][d] * W[r][ii][1 + d];
+          vp += gv0[r] * W[r][ii][0] + rhoc2 * gw;
+#pragma unroll
+          for (int d = 0; d < D; ++d) vv[d] += gv0[r] * W[r][ii][1 + d] + g[r][d] * W[r][ii][0] * inv_rho0;
+        }
+        Lv[ii][0] = vp;
+#pragma unroll
+        for (int d = 0; d < D; ++d) Lv[ii][1 + d] = vv[d];
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- face numerical fluxes (in place of the gathered traces) ----
+    for (int q8 = tid; q8 < ET * NK; q8 += NT) {
+      const int el = q8 / NK, k = q8 - el * NK;
+      const int f = k / NFP;
+      const int node = sFm[k];
+      T um[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) um[q] = sY[(q * ET + el) * NP + node];
+      const int nbr = sGI[el * RECI + f];
+      const int code = sGI[el * RECI + NF + f];
+      const T* gf = sGF + el * RECF + D * D + f * (D + 1);
+      T n[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) n[d] = gf[d];
+      const T sJ = gf[D];
+      T* slot = sN + ((size_t)el * NK + k) * C::Q4;
+      T h[NV];
+      if (code & kCodeBoundary) {
+        const T* B = a.bmat + (int64_t)nbr * NV * NV;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          T acc = 0;
+#pragma unroll
+          for (int qq = 0; qq < NV; ++qq) acc += __ldg(B + q * NV + qq) * um[qq];
+          h[q] = acc;
+        }
+      } else {
+        T up[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) up[q] = slot[q];
+        const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
+        T vn0 = v0x * n[0] + v0y * n[1];
+        if (D == 3) vn0 += v0z * n[2];
+        T avg[NV], dif[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
+        T nv = n[0] * avg[1] + n[1] * avg[2];
+        if (D == 3) nv += n[2] * avg[3];
+        h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
+#pragma unroll
+        for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
+      }
+#pragma unroll
+      for (int q = 0; q < NV; ++q) slot[q] = sJ * h[q];
+    }
+    __syncthreads();
+
+    // ---- lifting ----
+    {
+      const T* hrow = sN + (size_t)e * NK * C::Q4;
+#pragma unroll 4
+      for (int k = 0; k < NK; ++k) {
+        T hq[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) hq[q] = hrow[k * C::Q4 + q];
+        const T* lrow = sL + k * NP;
+#pragma unroll
+        for (int ii = 0; ii < NC; ++ii) {
+          const int i = (i0 + ii < NP) ? i0 + ii : NP - 1;
+          const T lv = lrow[i];
+#pragma unroll
+          for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv * hq[q];
+        }
+      }
+    }
+
+    // ---- RK update from registers ----
+    if (nepi > 0 && ok && !mbar_wait(&bar[2], it & 1)) ok = false;
+    const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
+    const T* ea = sE + (size_t)NV * ET * NP;
+    const T* es = sE + (size_t)2 * NV * ET * NP;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+#pragma unroll
+      for (int ii = 0; ii < NC; ++ii) {
+        const int i = i0 + ii;
+        if (i >= NP) continue;
+        const int lidx = (q * ET + e) * NP + i;
+        const int64_t g = q * stride + (e0 + e) * NP + i;
+        const T kv = dt * Lv[ii][q];
+        switch (stage) {
+          case 0:
+            a.k_out[g] = kv;
+            break;
+          case 1:
+            a.acc[g] = kv;
+            a.y_out[g] = eu[lidx] + (T)0.5 * kv;
+            break;
+          case 2:
+            a.acc[g] = ea[lidx] + (T)2 * kv;
+            a.y_out[g] = eu[lidx] + (T)0.5 * kv;
+            break;
+          case 3:
+            a.acc[g] = ea[lidx] + (T)2 * kv;
+            a.y_out[g] = eu[lidx] + kv;
+            break;
+          case 4: {
+            const T un = eu[lidx] + (ea[lidx] + kv) / (T)6;
+            a.u[g] = un;
+            const double sn = (double)es[lidx];
+            const double dn = sn - (double)un;
+            if (q == 0) {
+              red[0] += dn * dn;
+              const double dr = sn / a.c0sq - (double)un / a.c0sq;
+              red[1] += dr * dr;
+            } else {
+              red[1 + q] += dn * dn;
+            }
+            break;
+          }
+          default:
+            a.y_out[g] = eu[lidx] + kv;
+            break;
+        }
+      }
+    }
+    __syncthreads();  // buffers of this tile are free again
+  }
+  if (!ok) atomicOr(err, 1);
+
+  if (stage == 4) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      double v = red[c];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if ((tid & 31) == 0) sRed[(tid >> 5) * 5 + c] = v;
+    }
+    __syncthreads();
+    if (tid < 5) {
+      double v = 0.0;
+      for (int w = 0; w < NT / 32; ++w) v += sRed[w * 5 + tid];
+      a.partials[blockIdx.x * 5 + tid] = v;
+    }
+  }
+}
+
+template <typename T, int D, int P, int NC_, int ET_>
+struct Stage2 {
+  using C = Pipe<T, D, P, NC_, ET_>;
+  static cudaError_t launch(const StageArgs<T>& a, int grid, int* err, cudaStream_t s) {
+    auto kfn = stage2_kernel<T, D, P, NC_, ET_>;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    kfn<<<grid, C::NT, C::bytes, s>>>(a, err);
+    return cudaGetLastError();
+  }
+  static int blocks_per_sm() {
+    auto kfn = stage2_kernel<T, D, P, NC_, ET_>;
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, C::NT, C::bytes) != cudaSuccess) return 0;
+    return nb;
+  }
+};
+
+}  // namespace dgk

@@ -1,5 +1,7 @@
-// Instantiations of the fused stage kernel: double, 2-D, orders 1..4.
+// Instantiations of the fused stage kernels: double, 2-D, orders 1..4.
+// Generated variant table: (nodes per thread NC, elements per tile ET).
 #include "stage.cuh"
+#include "stage2.cuh"
 
 namespace dgk {
 
@@ -21,6 +23,30 @@ int blocks_per_sm_f64_2d(int order) {
     case 4: return blocks_per_sm_impl<double, 2, 4>();
   }
   return 1;
+}
+
+cudaError_t launch_stage2_f64_2d(int order, int variant, const StageArgs<double>& a, int grid, int* err, cudaStream_t s) {
+  if (order == 1 && variant == 0) return Stage2<double, 2, 1, 3, 128>::launch(a, grid, err, s);
+  if (order == 2 && variant == 0) return Stage2<double, 2, 2, 6, 128>::launch(a, grid, err, s);
+  if (order == 2 && variant == 1) return Stage2<double, 2, 2, 3, 64>::launch(a, grid, err, s);
+  if (order == 3 && variant == 0) return Stage2<double, 2, 3, 5, 64>::launch(a, grid, err, s);
+  if (order == 3 && variant == 1) return Stage2<double, 2, 3, 4, 32>::launch(a, grid, err, s);
+  if (order == 3 && variant == 2) return Stage2<double, 2, 3, 2, 32>::launch(a, grid, err, s);
+  if (order == 4 && variant == 0) return Stage2<double, 2, 4, 5, 32>::launch(a, grid, err, s);
+  if (order == 4 && variant == 1) return Stage2<double, 2, 4, 4, 32>::launch(a, grid, err, s);
+  return cudaErrorInvalidValue;
+}
+
+Stage2Info stage2_info_f64_2d(int order, int variant) {
+  if (order == 1 && variant == 0) { using C = Pipe<double, 2, 1, 3, 128>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 1, 3, 128>::blocks_per_sm(), 1}; }
+  if (order == 2 && variant == 0) { using C = Pipe<double, 2, 2, 6, 128>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 2, 6, 128>::blocks_per_sm(), 2}; }
+  if (order == 2 && variant == 1) { using C = Pipe<double, 2, 2, 3, 64>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 2, 3, 64>::blocks_per_sm(), 2}; }
+  if (order == 3 && variant == 0) { using C = Pipe<double, 2, 3, 5, 64>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 3, 5, 64>::blocks_per_sm(), 3}; }
+  if (order == 3 && variant == 1) { using C = Pipe<double, 2, 3, 4, 32>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 3, 4, 32>::blocks_per_sm(), 3}; }
+  if (order == 3 && variant == 2) { using C = Pipe<double, 2, 3, 2, 32>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 3, 2, 32>::blocks_per_sm(), 3}; }
+  if (order == 4 && variant == 0) { using C = Pipe<double, 2, 4, 5, 32>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 4, 5, 32>::blocks_per_sm(), 2}; }
+  if (order == 4 && variant == 1) { using C = Pipe<double, 2, 4, 4, 32>; return Stage2Info{C::NC, C::ET, C::NT, (int)C::bytes, Stage2<double, 2, 4, 4, 32>::blocks_per_sm(), 2}; }
+  return Stage2Info{0, 0, 0, 0, 0, 0};
 }
 
 }  // namespace dgk

@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps"]
+           "dg_bench_steps", "dg_tune"]
 
 
 class MeshDesc(C.Structure):
@@ -38,7 +38,7 @@ class Info(C.Structure):
     _fields_ = [("dim", C.c_int), ("order", C.c_int), ("nodes_per_elem", C.c_int), ("n_var", C.c_int),
                 ("precision", C.c_int), ("n_elems", C.c_int64), ("n_faces", C.c_int64),
                 ("n_boundary_faces", C.c_int64), ("penalty_sign_hist", C.c_int64 * 2),
-                ("device_bytes", C.c_int64), ("setup_ms", C.c_double)]
+                ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("kernel_variant", C.c_int)]
 
 
 def lib():
@@ -70,6 +70,7 @@ def lib():
         L.dg_stream.argtypes = [C.c_void_p]
         L.dg_stream.restype = C.c_void_p
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
+        L.dg_tune.argtypes = [C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -205,6 +206,10 @@ class Solver:
         self._ck(lib().dg_face_info(self.h, _ip(nbr), pen.ctypes.data_as(C.POINTER(C.c_int)),
                                     bc.ctypes.data_as(C.POINTER(C.c_int))), "dg_face_info")
         return dict(nbr=nbr.reshape(-1, nf), penalty=pen.reshape(-1, nf), bc=bc.reshape(-1, nf))
+
+    def tune(self, variant=-2):
+        self._ck(lib().dg_tune(self.h, variant), "dg_tune")
+        return self.info()["kernel_variant"]
 
     def stream(self):
         return lib().dg_stream(self.h)

@@ -89,6 +89,7 @@ typedef struct {
   int64_t penalty_sign_hist[2]; /* interior faces with s_f = -1, +1 */
   int64_t device_bytes;
   double setup_ms;
+  int kernel_variant; /* stage kernel in use: -1 baseline, k >= 0 pipelined variant k */
 } dg_info_t;
 
 int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out);
@@ -126,6 +127,14 @@ int dg_cell_means(dg_ctx* ctx, double* p, double* rho, double* v);
  * neighbour element (-1 on the boundary), penalty sign s_f (0 on the
  * boundary) and BC code (1 reflecting, 0 absorbing, -1 interior). */
 int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
+
+/* Stage kernel selection. variant -2: time every variant on this mesh and
+ * keep the fastest (what dg_create does; the environment variable
+ * DGFEM_STAGE_VARIANT overrides it there); -1: baseline kernel; k >= 0:
+ * pipelined variant k (TMA-staged tiles; the variants differ in output nodes
+ * per thread and elements per tile). Returns DG_ERR_ARG for a variant that
+ * does not exist for this element type. */
+int dg_tune(dg_ctx* ctx, int variant);
 
 /* The CUDA stream (cudaStream_t) all work of ctx is issued on. */
 void* dg_stream(dg_ctx* ctx);

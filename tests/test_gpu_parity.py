@@ -28,6 +28,18 @@ def _mesh(pkg, dim, p, reflect=True):
     return dict(dim=dim, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"], groups=groups)
 
 
+def kernel_variants(pkg, S):
+    """-1 (baseline kernel) and every pipelined variant available for S."""
+    out = [-1]
+    for v in range(8):
+        try:
+            S.tune(v)
+        except pkg.gpu.SolverError:
+            break
+        out.append(v)
+    return out
+
+
 def _phys(dim):
     v0 = PHYS["v0"] if dim == 3 else (PHYS["v0"][0], PHYS["v0"][1], 0.0)
     return dict(v0=v0, rho0=PHYS["rho0"], c0=PHYS["c0"])
@@ -43,13 +55,15 @@ def test_rhs_parity(pkg, oracle, dim, p, prec):
     dt = 1e-4
     ref = oracle.Problem(mesh, dt=dt, **ph).stage(u)
     S = pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
-    k = S.rhs(u, dt)
     tol = 5e-11 if prec == "fp64" else 5e-4
     nv = dim + 1
-    err = rel_l2(k[:nv], ref[:nv])
-    assert err <= tol, (dim, p, prec, err)
-    if dim == 2:
-        assert np.all(k[3] == 0.0)
+    for v in kernel_variants(pkg, S):
+        S.tune(v)
+        k = S.rhs(u, dt)
+        err = rel_l2(k[:nv], ref[:nv])
+        assert err <= tol, (dim, p, prec, v, err)
+        if dim == 2:
+            assert np.all(k[3] == 0.0)
 
 
 @pytest.mark.parametrize("dim,p", [(2, 2), (3, 2), (3, 3)])
@@ -81,8 +95,9 @@ def _sources_observers(mesh, srcs, obs):
     return sdofs, odofs, ows
 
 
-@pytest.mark.parametrize("dim,p,prec", [(2, 3, "fp64"), (3, 2, "fp64"), (2, 3, "fp32"), (3, 3, "fp32")])
-def test_run_parity(pkg, oracle, dim, p, prec):
+@pytest.mark.parametrize("variant", [-1, 0, 1])
+@pytest.mark.parametrize("dim,p,prec", [(2, 3, "fp64"), (3, 2, "fp64"), (3, 3, "fp64"), (2, 3, "fp32"), (3, 3, "fp32")])
+def test_run_parity(pkg, oracle, dim, p, prec, variant):
     mesh = _mesh(pkg, dim, p)
     ph = _phys(dim)
     dt, nsteps = 2e-4, 40
@@ -94,6 +109,7 @@ def test_run_parity(pkg, oracle, dim, p, prec):
     ref = P.run()
     assert ref["steps"] == nsteps
     S = pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
+    S.tune(variant)
     S.set_state(P.initial_state())
     sdofs, odofs, ows = _sources_observers(mesh, [src], obs)
     S.set_sources(sdofs)
