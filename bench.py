@@ -150,6 +150,8 @@ def run_gpu(args, rank, world):
     prec = pkg.gpu.DG_FP32 if args.precision == "fp32" else pkg.gpu.DG_FP64
     W = WORKLOAD
     S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=prec, device=device)
+    if args.variant != -2:
+        S.tune(args.variant)
     info = S.info()
     E, np_ = mesh["elem_nodes"].shape
     nv = 4
@@ -211,6 +213,7 @@ def run_gpu(args, rank, world):
                      "kernel_ms_per_step": kern_ms, "algorithmic_bytes_per_step": int(alg_bytes)},
         "clocks": clk.summary(),
         "setup_ms": info["setup_ms"],
+        "kernel_variant": info["kernel_variant"],
     }
     S.close()
     return line
@@ -224,6 +227,8 @@ def run_profile(args):
     W = WORKLOAD
     prec = pkg.gpu.DG_FP32 if args.precision == "fp32" else pkg.gpu.DG_FP64
     S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=prec, device=0)
+    if args.variant != -2:
+        S.tune(args.variant)
     sdofs, odofs, ows = node_sets(mesh, src, obs)
     S.set_sources(sdofs)
     n = args.warmup + args.steps
@@ -281,6 +286,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=-2,
+                    help="stage kernel variant (-2: autotuned at setup, -1: baseline kernel, k: pipelined variant k)")
     ap.add_argument("--profile", action="store_true",
                     help="only build the workload and run warmup + steps time steps (for ncu captures)")
     args = ap.parse_args()
