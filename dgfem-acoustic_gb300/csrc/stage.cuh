@@ -308,9 +308,15 @@ template <typename T, int D, int P>
 int blocks_per_sm_impl() {
   using M = StageSmem<T, D, P>;
   auto kfn = stage_kernel<T, D, P>;
-  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M::bytes);
+  if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M::bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, ShapeT<D, P, T>::NT, M::bytes) != cudaSuccess) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, ShapeT<D, P, T>::NT, M::bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
   return nb < 1 ? 1 : nb;
 }
 

@@ -431,9 +431,17 @@ struct Stage2 {
   }
   static int blocks_per_sm() {
     auto kfn = stage2_kernel<T, D, P, NC_, ET_>;
-    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) return 0;
+    // a configuration larger than the shared memory of an SM is reported as
+    // unavailable; the failed query must not leave a sticky launch error
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, C::NT, C::bytes) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, C::NT, C::bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
     return nb;
   }
 };
