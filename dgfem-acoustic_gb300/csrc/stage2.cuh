@@ -78,6 +78,37 @@ __device__ __forceinline__ void cp_async_commit_wait_all() {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// VW-wide vector load/store of T (VW in {1, 2, 4}; addresses VW-aligned).
+template <typename T, int VW>
+__device__ __forceinline__ void vload(T* r, const T* p) {
+  if constexpr (VW == 4 && sizeof(T) == 4) {
+    float4 v = *reinterpret_cast<const float4*>(p);
+    r[0] = v.x, r[1] = v.y, r[2] = v.z, r[3] = v.w;
+  } else if constexpr (VW == 2 && sizeof(T) == 4) {
+    float2 v = *reinterpret_cast<const float2*>(p);
+    r[0] = v.x, r[1] = v.y;
+  } else if constexpr (VW == 2 && sizeof(T) == 8) {
+    double2 v = *reinterpret_cast<const double2*>(p);
+    r[0] = v.x, r[1] = v.y;
+  } else {
+#pragma unroll
+    for (int v = 0; v < VW; ++v) r[v] = p[v];
+  }
+}
+template <typename T, int VW>
+__device__ __forceinline__ void vstore(T* p, const T* r) {
+  if constexpr (VW == 4 && sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
+  } else if constexpr (VW == 2 && sizeof(T) == 4) {
+    *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
+  } else if constexpr (VW == 2 && sizeof(T) == 8) {
+    *reinterpret_cast<double2*>(p) = make_double2(r[0], r[1]);
+  } else {
+#pragma unroll
+    for (int v = 0; v < VW; ++v) p[v] = r[v];
+  }
+}
+
 template <int N, int A>
 struct RoundUp {
   static constexpr int v = (N + A - 1) / A * A;
@@ -95,6 +126,10 @@ struct Pipe {
   static constexpr int NT = ET * NSPLIT;
   static constexpr int RECF = S::RECF, RECI = S::RECI;
   static constexpr int Q4 = 4;  // variables per face node slot (vz slot unused in 2-D)
+  // epilogue vector width: chunks of NC nodes start on VW-element boundaries
+  // when NP is a multiple of NC (16-byte vectors at most)
+  static constexpr int VWMAX = 16 / (int)sizeof(T);
+  static constexpr int VW = (NP % NC != 0) ? 1 : (NC % 4 == 0 && VWMAX >= 4) ? 4 : (NC % 2 == 0) ? 2 : 1;
   // byte sizes of the TMA segments
   static constexpr uint32_t YSEG = ET * NP * sizeof(T);  // one variable of the tile
   static constexpr uint32_t GFB = ET * RECF * sizeof(T);
@@ -344,52 +379,71 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       }
     }
 
-    // ---- RK update from registers ----
+    // ---- RK update from registers (vectorised when the node chunk allows) ----
     if (nepi > 0 && ok && !mbar_wait(&bar[2], it & 1)) ok = false;
     const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
     const T* ea = sE + (size_t)NV * ET * NP;
     const T* es = sE + (size_t)2 * NV * ET * NP;
+    constexpr int VW = C::VW;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
 #pragma unroll
-      for (int ii = 0; ii < NC; ++ii) {
-        const int i = i0 + ii;
+      for (int c0 = 0; c0 < NC; c0 += VW) {
+        const int i = i0 + c0;
         if (i >= NP) continue;
         const int lidx = (q * ET + e) * NP + i;
         const int64_t g = q * stride + (e0 + e) * NP + i;
-        const T kv = dt * Lv[ii][q];
+        T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
+#pragma unroll
+        for (int v = 0; v < VW; ++v) kv[v] = dt * Lv[c0 + v][q];
         switch (stage) {
           case 0:
-            a.k_out[g] = kv;
+            vstore<T, VW>(a.k_out + g, kv);
             break;
           case 1:
-            a.acc[g] = kv;
-            a.y_out[g] = eu[lidx] + (T)0.5 * kv;
+            vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+            for (int v = 0; v < VW; ++v) o1[v] = kv[v], o2[v] = xu[v] + (T)0.5 * kv[v];
+            vstore<T, VW>(a.acc + g, o1);
+            vstore<T, VW>(a.y_out + g, o2);
             break;
           case 2:
-            a.acc[g] = ea[lidx] + (T)2 * kv;
-            a.y_out[g] = eu[lidx] + (T)0.5 * kv;
-            break;
           case 3:
-            a.acc[g] = ea[lidx] + (T)2 * kv;
-            a.y_out[g] = eu[lidx] + kv;
+            vload<T, VW>(xu, eu + lidx);
+            vload<T, VW>(xa, ea + lidx);
+#pragma unroll
+            for (int v = 0; v < VW; ++v)
+              o1[v] = xa[v] + (T)2 * kv[v], o2[v] = xu[v] + (stage == 2 ? (T)0.5 * kv[v] : kv[v]);
+            vstore<T, VW>(a.acc + g, o1);
+            vstore<T, VW>(a.y_out + g, o2);
             break;
           case 4: {
-            const T un = eu[lidx] + (ea[lidx] + kv) / (T)6;
-            a.u[g] = un;
-            const double sn = (double)es[lidx];
-            const double dn = sn - (double)un;
-            if (q == 0) {
-              red[0] += dn * dn;
-              const double dr = sn / a.c0sq - (double)un / a.c0sq;
-              red[1] += dr * dr;
-            } else {
-              red[1 + q] += dn * dn;
+            T xs[VW];
+            vload<T, VW>(xu, eu + lidx);
+            vload<T, VW>(xa, ea + lidx);
+            vload<T, VW>(xs, es + lidx);
+#pragma unroll
+            for (int v = 0; v < VW; ++v) {
+              const T un = xu[v] + (xa[v] + kv[v]) / (T)6;
+              o1[v] = un;
+              const double sn = (double)xs[v];
+              const double dn = sn - (double)un;
+              if (q == 0) {
+                red[0] += dn * dn;
+                const double dr = sn / a.c0sq - (double)un / a.c0sq;
+                red[1] += dr * dr;
+              } else {
+                red[1 + q] += dn * dn;
+              }
             }
+            vstore<T, VW>(a.u + g, o1);
             break;
           }
           default:
-            a.y_out[g] = eu[lidx] + kv;
+            vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+            for (int v = 0; v < VW; ++v) o2[v] = xu[v] + kv[v];
+            vstore<T, VW>(a.y_out + g, o2);
             break;
         }
       }
