@@ -109,6 +109,20 @@ __device__ __forceinline__ void vstore(T* p, const T* r) {
   }
 }
 
+// The NC entries row[i0 .. i0+NC) of an operator row in shared memory, in
+// VW-wide vectors when the chunk is aligned; entries past the row end
+// (last chunk of a node split that does not divide NP) repeat the last entry.
+template <typename T, int NC, int VW, int NP>
+__device__ __forceinline__ void load_chunk(T* out, const T* row, int i0) {
+  if constexpr (VW > 1) {
+#pragma unroll
+    for (int c = 0; c < NC; c += VW) vload<T, VW>(out + c, row + i0 + c);
+  } else {
+#pragma unroll
+    for (int ii = 0; ii < NC; ++ii) out[ii] = row[(i0 + ii < NP) ? i0 + ii : NP - 1];
+  }
+}
+
 template <int N, int A>
 struct RoundUp {
   static constexpr int v = (N + A - 1) / A * A;
@@ -144,8 +158,11 @@ struct Pipe {
   static constexpr size_t oGF = oY + 2 * (size_t)NV * YSEG;                  // 2 x [ET][RECF]
   static constexpr size_t oGI = oGF + 2 * (size_t)GFB;                        // 2 x [ET][RECI]
   static constexpr size_t oE = RoundUp<oGI + 2 * (size_t)GIB, 128>::v;       // [3][NV][ET][NP]
-  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                    // [ET][NK][4]
-  static constexpr size_t oR = RoundUp<oN + (size_t)ET * NK * Q4 * sizeof(T), 16>::v;  // [NT/32][5] double
+  // neighbour traces / face fluxes: one plane per variable, element stride
+  // NKP odd so that reads of one face node across elements hit distinct banks
+  static constexpr int NKP = NK | 1;
+  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                    // [NV][ET][NKP]
+  static constexpr size_t oR = RoundUp<oN + (size_t)NV * ET * NKP * sizeof(T), 16>::v;  // [NT/32][5] double
   static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
   static_assert(NT % 32 == 0, "threads per block must be a multiple of 32");
   static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
@@ -239,13 +256,13 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
         const int nbr = sGI[el * RECI + f];
         const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
         const T* src = a.y_in + (int64_t)nbr * NP + nn;
-        T* dst = sN + ((size_t)el * NK + k) * C::Q4;
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
+          T* dst = sN + (size_t)(q * ET + el) * C::NKP + k;
           if (sizeof(T) == 4)
-            cp_async4(dst + q, src + q * stride);
+            cp_async4(dst, src + q * stride);
           else
-            cp_async8(dst + q, src + q * stride);
+            cp_async8(dst, src + q * stride);
         }
       }
     }
@@ -269,14 +286,12 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
         for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
 #pragma unroll
         for (int r = 0; r < D; ++r) {
-          const T* drow = sD + (r * NP + j) * NP;
+          T dv[NC];
+          load_chunk<T, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
 #pragma unroll
-          for (int ii = 0; ii < NC; ++ii) {
-            const int i = (i0 + ii < NP) ? i0 + ii : NP - 1;
-            const T dv = drow[i];
+          for (int ii = 0; ii < NC; ++ii)
 #pragma unroll
-            for (int q = 0; q < NV; ++q) W[r][ii][q] += dv * yq[q];
-          }
+            for (int q = 0; q < NV; ++q) W[r][ii][q] += dv[ii] * yq[q];
         }
       }
       const T* G = sGF + e * RECF;
@@ -328,7 +343,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
 #pragma unroll
       for (int d = 0; d < D; ++d) n[d] = gf[d];
       const T sJ = gf[D];
-      T* slot = sN + ((size_t)el * NK + k) * C::Q4;
+      T* slot = sN + (size_t)el * C::NKP + k;  // variable q at slot[q * ET * NKP]
       T h[NV];
       if (code & kCodeBoundary) {
         const T* B = a.bmat + (int64_t)nbr * NV * NV;
@@ -342,7 +357,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       } else {
         T up[NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) up[q] = slot[q];
+        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
         const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
         T vn0 = v0x * n[0] + v0y * n[1];
         if (D == 3) vn0 += v0z * n[2];
@@ -356,26 +371,24 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
         for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
       }
 #pragma unroll
-      for (int q = 0; q < NV; ++q) slot[q] = sJ * h[q];
+      for (int q = 0; q < NV; ++q) slot[(size_t)q * ET * C::NKP] = sJ * h[q];
     }
     __syncthreads();
 
     // ---- lifting ----
     {
-      const T* hrow = sN + (size_t)e * NK * C::Q4;
+      const T* hrow = sN + (size_t)e * C::NKP;
 #pragma unroll 4
       for (int k = 0; k < NK; ++k) {
         T hq[NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) hq[q] = hrow[k * C::Q4 + q];
-        const T* lrow = sL + k * NP;
+        for (int q = 0; q < NV; ++q) hq[q] = hrow[(size_t)q * ET * C::NKP + k];
+        T lv[NC];
+        load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
 #pragma unroll
-        for (int ii = 0; ii < NC; ++ii) {
-          const int i = (i0 + ii < NP) ? i0 + ii : NP - 1;
-          const T lv = lrow[i];
+        for (int ii = 0; ii < NC; ++ii)
 #pragma unroll
-          for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv * hq[q];
-        }
+          for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv[ii] * hq[q];
       }
     }
 
