@@ -435,6 +435,8 @@ int select_variant(dg_ctx* c, int want) {
 }  // namespace
 
 namespace dgc {
+void set_global_error(const std::string& m) { g_create_error = m; }
+
 cudaError_t dev_alloc(dg_ctx* c, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes + 64);
   if (e == cudaSuccess) {

@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune"]
+           "dg_bench_steps", "dg_tune", "dg_residuals_noalloc"]
 
 
 class MeshDesc(C.Structure):
@@ -71,6 +71,8 @@ def lib():
         L.dg_stream.restype = C.c_void_p
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
         L.dg_tune.argtypes = [C.c_void_p, C.c_int]
+        L.dg_residuals_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, I64, I64, D, C.c_void_p,
+                                           C.c_void_p]
         _lib = L
     return _lib
 
@@ -93,6 +95,15 @@ def _csr(lists, dtype=np.int64):
 
 class SolverError(RuntimeError):
     pass
+
+
+def residuals_noalloc(u_ptr, snap_ptr, precision, n_var, n_per_var, var_stride, c0, res_ptr, stream=None):
+    """dg_residuals_noalloc on caller-owned device pointers (ints); raises on error."""
+    L = lib()
+    rc = L.dg_residuals_noalloc(C.c_void_p(u_ptr), C.c_void_p(snap_ptr), precision, n_var, n_per_var, var_stride,
+                                c0, C.c_void_p(res_ptr), C.c_void_p(stream) if stream else None)
+    if rc != 0:
+        raise SolverError("dg_residuals_noalloc: %s: %s" % (ERRORS.get(rc, rc), L.dg_last_error(None).decode()))
 
 
 class Solver:

@@ -146,6 +146,30 @@ void* dg_stream(dg_ctx* ctx);
 int dg_bench_steps(dg_ctx* ctx, int64_t n_steps, double dt, int64_t flush_bytes, double* step_ms,
                    double* kernel_ms);
 
+/* Allocation-free residual diagnostic. No counterpart in the reference: it
+ * serves callers that cannot allocate device memory where they need the
+ * diagnostic (code inside a host framework that owns every allocation, loops
+ * that must not call the allocator, callers that manage their own device
+ * buffers). It needs no context.
+ *
+ * Computes, on `stream`, the five residual means of the reference's time loop
+ * between a state u and a snapshot (res[0] p, res[1] p/c0^2, res[2..4] vx, vy,
+ * vz; variables beyond n_var give 0) from caller-owned device arrays laid out
+ * as n_var planes of var_stride elements (float for DG_FP32, double for
+ * DG_FP64), each with n_per_var nodes, and writes them to the caller-owned
+ * device array res[5]. It allocates nothing and does not synchronise.
+ *
+ * Its only scratch is a fixed 160 KiB array inside the library that every GPU
+ * loading the library holds until the process exits; n_per_var is therefore
+ * limited to 67,108,864 nodes (DG_ERR_ARG beyond). The first call on a device
+ * looks up that array's device address with the device current; make that
+ * first call before any stream capture. All calls share the array, so calls
+ * that overlap on the GPU (concurrent streams) race; calls in one stream are
+ * safe back to back (each call writes every scratch row it reads). Errors are
+ * reported through dg_last_error(NULL). */
+int dg_residuals_noalloc(const void* u, const void* snap, int precision, int n_var, int64_t n_per_var,
+                         int64_t var_stride, double c0, double* res, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
