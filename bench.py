@@ -219,6 +219,115 @@ def run_gpu(args, rank, world):
     return line
 
 
+ENSEMBLE = dict(name="batched ensemble: 256 2-D LEE instances, 1k-50k tris, p in {2,3,4}", n=256, seed=4,
+                half_width=5.0, rho0=1.225, c0=340.0, cfl=0.5, jitter=0.2,
+                observers=[(2.5, 2.5, 0.0, 0.3), (-2.5, 2.5, 0.0, 0.3), (-2.5, -2.5, 0.0, 0.3), (2.5, -2.5, 0.0, 0.3)])
+
+
+def ensemble_instances(n=None, seed=None):
+    """Seeded draws of the ensemble workload: element count log-uniform in
+    [1e3, 5e4] (grid n = ceil(sqrt(E/2))), order uniform in {2,3,4}, monopole
+    position uniform in [-4,4]^2, frequency uniform in [20,400] Hz, Mach
+    uniform in [0,0.3] in a uniform direction, all sides Absorbing, dt from
+    CFL 0.5."""
+    pkg = _pkg()
+    W = ENSEMBLE
+    n = n or W["n"]
+    rng = np.random.default_rng(W["seed"] if seed is None else seed)
+    out = []
+    for k in range(n):
+        E = float(np.exp(rng.uniform(np.log(1e3), np.log(5e4))))
+        grid = int(np.ceil(np.sqrt(E / 2)))
+        p = int(rng.integers(2, 5))
+        sx, sy = rng.uniform(-4, 4, 2)
+        f = rng.uniform(20, 400)
+        M = rng.uniform(0, 0.3)
+        th = rng.uniform(0, 2 * np.pi)
+        v0 = (M * W["c0"] * np.cos(th), M * W["c0"] * np.sin(th), 0.0)
+        m = pkg.meshgen.square(n=grid, order=p, half_width=W["half_width"], jitter=W["jitter"],
+                               seed=int(rng.integers(1 << 30)))
+        mesh = dict(dim=2, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                    groups=pkg.meshgen.solver_groups(m, {"Absorbing": "Absorbing"}))
+        h = 2 * W["half_width"] / grid * (1 - 2 * W["jitter"])
+        dt = W["cfl"] * h / ((W["c0"] + np.linalg.norm(v0)) * (2 * p + 1))
+        src = [sx, sy, 0.0, 0.2, 0.1, f, 0.0, 1e9]
+        out.append(dict(mesh=mesh, v0=v0, dt=dt, src=src, obs=W["observers"], p=p))
+    return out
+
+
+def run_ensemble(args):
+    """Aggregate DOF-updates/s of the batched path over the ensemble, the
+    plain single-instance path on a sample of the same instances, and the
+    per-instance FP32 error against the FP64 batch."""
+    pkg = _pkg()
+    t0 = time.perf_counter()
+    insts = ensemble_instances()
+    gen_s = time.perf_counter() - t0
+    W = ENSEMBLE
+
+    def make(prec, subset):
+        B = pkg.gpu.Batch([dict(mesh=i["mesh"], v0=i["v0"], dt=i["dt"]) for i in subset], rho0=W["rho0"],
+                          c0=W["c0"], precision=prec)
+        for k, i in enumerate(subset):
+            sd, od, ow = node_sets(i["mesh"], i["src"], i["obs"])
+            n = args.warmup + args.steps + 2
+            t = np.arange(n) * i["dt"]
+            B.set_sources(k, sd, (i["src"][4] * np.sin(2 * np.pi * i["src"][5] * t))[:, None])
+            B.set_observers(k, od, ow)
+        return B
+
+    dofs = sum(i["mesh"]["elem_nodes"].size * 3 for i in insts)
+    B = make(pkg.gpu.DG_FP32, insts)
+    B.run(args.warmup)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms = B.bench(args.steps)
+    batched = dofs / (ms * 1e-3)
+    B.close()
+    # plain path: every 32nd instance on its own, same steps
+    sample = insts[::32]
+    tot_dof, tot_ms = 0, 0.0
+    for i in sample:
+        S = pkg.gpu.Solver(i["mesh"], v0=i["v0"], rho0=W["rho0"], c0=W["c0"], precision=pkg.gpu.DG_FP32)
+        sd, od, ow = node_sets(i["mesh"], i["src"], i["obs"])
+        S.set_sources(sd)
+        t = np.arange(args.warmup + 3 * args.steps + 8) * i["dt"]
+        S.set_source_values((i["src"][4] * np.sin(2 * np.pi * i["src"][5] * t))[:, None])
+        S.set_observers(od, ow)
+        S.snapshot()
+        S.run(args.warmup, i["dt"])
+        sm, _ = S.bench_steps(args.steps, i["dt"], flush_bytes=0, kernel_time=False)
+        tot_dof += i["mesh"]["elem_nodes"].size * 3
+        tot_ms += sm
+        S.close()
+    plain = tot_dof / (tot_ms * 1e-3)
+    # accuracy: FP32 vs FP64 batch on every 8th instance
+    sub = insts[::8]
+    nerr = min(args.steps, 100)
+    res = []
+    for prec in (pkg.gpu.DG_FP64, pkg.gpu.DG_FP32):
+        B = make(prec, sub)
+        for k, i in enumerate(sub):
+            x = i["mesh"]["xyz"][i["mesh"]["elem_nodes"].reshape(-1)]
+            u = np.zeros((4, x.shape[0]))
+            u[0] = np.exp(-((x[:, 0] - i["src"][0]) ** 2 + (x[:, 1] - i["src"][1]) ** 2) / 0.5)
+            B.set_state(k, u)
+        B.run(nerr)
+        res.append([B.get_state(k) for k in range(len(sub))])
+        B.close()
+    errs = [float(np.linalg.norm(a[:3] - b[:3]) / np.linalg.norm(b[:3])) for a, b in zip(res[1], res[0])]
+    return {"metric": "RK4 DOF-updates/s (batched ensemble)", "value": batched, "unit": UNIT,
+            "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
+            "config": {"workload": W["name"], "instances": len(insts), "dofs": int(dofs),
+                       "elements": int(sum(i["mesh"]["elem_nodes"].shape[0] for i in insts)),
+                       "orders": {str(p): sum(1 for i in insts if i["p"] == p) for p in (2, 3, 4)},
+                       "generation_s": gen_s},
+            "plain_single_instance": {"value": plain, "unit": UNIT, "sample": "%d instances run one by one"
+                                      % len(sample)},
+            "batched_over_plain": batched / plain,
+            "fp32_vs_fp64_rel_l2_max": max(errs), "error_steps": nerr, "error_instances": len(sub),
+            "clocks": clk.summary()}
+
+
 def run_profile(args):
     """Warm-up plus a few RK4 steps of the workload through the per-step graph,
     nothing else (the command line that the ncu summaries in profiles/ use)."""
@@ -288,6 +397,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=-2,
                     help="stage kernel variant (-2: autotuned at setup, -1: baseline kernel, k: pipelined variant k)")
+    ap.add_argument("--workload", default="cube", choices=["cube", "ensemble"])
     ap.add_argument("--profile", action="store_true",
                     help="only build the workload and run warmup + steps time steps (for ncu captures)")
     args = ap.parse_args()
@@ -299,6 +409,10 @@ def main():
         dist.init_process_group("gloo")
     if args.profile:
         run_profile(args)
+        return
+    if args.workload == "ensemble" and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps(run_ensemble(args)), flush=True)
         return
     if args.impl == "reference":
         if rank == 0:

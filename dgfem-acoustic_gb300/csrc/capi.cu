@@ -436,6 +436,10 @@ int select_variant(dg_ctx* c, int want) {
 
 namespace dgc {
 void set_global_error(const std::string& m) { g_create_error = m; }
+cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) { return ::enqueue_step(c, kind, dt, ev); }
+int ensure_out_cap(dg_ctx* c, int64_t n) { return ::ensure_out_cap(c, n); }
+int create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, const double* elem_v0,
+               const double* elem_scale, dg_ctx** out, std::string* err);
 
 cudaError_t dev_alloc(dg_ctx* c, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes + 64);
@@ -452,10 +456,20 @@ extern "C" {
 const char* dg_last_error(const dg_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
 
 int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out) {
+  std::string e;
+  int rc = dgc::create_ctx(mesh, phys, precision, device, nullptr, nullptr, out, &e);
+  if (rc != DG_OK) g_create_error = e;
+  return rc;
+}
+
+}  // extern "C"
+
+int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, const double* elem_v0,
+                    const double* elem_scale, dg_ctx** out, std::string* err) {
   if (!out) return DG_ERR_ARG;
   *out = nullptr;
   auto bad = [&](int code, const std::string& m) {
-    g_create_error = m;
+    *err = m;
     return code;
   };
   if (!mesh || !phys || !mesh->xyz || !mesh->elem_nodes) return bad(DG_ERR_ARG, "null mesh or physics");
@@ -555,7 +569,7 @@ int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int 
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, c->stream);
-  int rc = dgc::run_setup(c, mesh);
+  int rc = dgc::run_setup(c, mesh, elem_v0, elem_scale);
   if (rc != DG_OK) {
     std::string m = c->err;
     dg_destroy(c);
@@ -644,6 +658,8 @@ int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int 
   *out = c;
   return DG_OK;
 }
+
+extern "C" {
 
 int dg_destroy(dg_ctx* c) {
   if (!c) return DG_OK;

@@ -77,7 +77,7 @@ struct dg_ctx {
 
 namespace dgc {
 // FP64 GPU setup of geometry, connectivity and boundary data (setup.cu).
-int run_setup(dg_ctx* c, const dg_mesh_desc* mesh);
+int run_setup(dg_ctx* c, const dg_mesh_desc* mesh, const double* elem_v0, const double* elem_scale);
 // Allocation helper that records the buffer for dg_destroy.
 cudaError_t dev_alloc(dg_ctx* c, void** p, size_t bytes);
 }  // namespace dgc

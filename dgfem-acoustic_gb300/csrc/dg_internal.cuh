@@ -4,7 +4,10 @@
 //   state   T [n_var][Epad*Np]  per variable, element-major, internal lattice
 //                               node order inside an element
 //   geoF    T [Epad][RECF]      G = d(xi)/dx (dim*dim), then per local face:
-//                               outward unit normal (dim) and sJ = J_f/|det J|
+//                               outward unit normal (dim) and sJ = J_f/|det J|,
+//                               then the element's mean flow v0 (dim) and its
+//                               time-step scale (1 for a single run; the
+//                               instance's dt in a batch)
 //   geoI    int [Epad][RECI]    per local face: neighbour element (interior)
 //                               or boundary-face index; then per local face the
 //                               face code (neighbour local face, corner
@@ -39,7 +42,8 @@ struct Shape {
   // ET * NSPLIT a multiple of the warp size
   static constexpr int ET = NSPLIT <= 2 ? 128 / NSPLIT : 32;
   static constexpr int NT = ET * NSPLIT;  // threads per block
-  static constexpr int RECF_RAW = D * D + NF * (D + 1);
+  static constexpr int PHYS_OFF = D * D + NF * (D + 1);  // v0 (D), dt scale
+  static constexpr int RECF_RAW = PHYS_OFF + D + 1;
   static constexpr int RECI = ((2 * NF) + 3) / 4 * 4;
 };
 

@@ -43,7 +43,11 @@ struct SetupDev {
   int ngroups;
   const int* gbc;
   const unsigned* gmask;  // [nnodes] bit g set: node in group g
+  const double* ev0;      // [E][3] per-element mean flow, or null (v0 above for all)
+  const double* escale;   // [E] per-element time-step scale, or null (1)
 };
+
+__device__ __forceinline__ const double* elem_v0(const SetupDev& s, int64_t e) { return s.ev0 ? s.ev0 + 3 * e : s.v0; }
 
 __device__ __forceinline__ const double* X(const SetupDev& s, int64_t node) { return s.xyz + 3 * node; }
 
@@ -259,7 +263,8 @@ __global__ void k_face_geom(SetupDev s, const double* det, const int64_t* partne
     for (int g = 0; g < s.ngroups; ++g)
       if ((m >> g) & 1u) bc = s.gbc[g] == 1 ? 1 : 0;
     bcode[b] = bc;
-    double v0n = s.v0[0] * n[0] + s.v0[1] * n[1] + s.v0[2] * n[2];
+    const double* v0 = elem_v0(s, e);
+    double v0n = v0[0] * n[0] + v0[1] * n[1] + v0[2] * n[2];
     double R[4][4];
     if (bc == 1) {
       // reflecting wall: remove the normal velocity of the trace, then n.F
@@ -310,11 +315,17 @@ __global__ void k_face_geom(SetupDev s, const double* det, const int64_t* partne
   geoI[e * reci + s.nf + lf] = code;
 }
 
-// Places G (d xi / dx) at the head of each element's geometry record.
-__global__ void k_place_G(int64_t E, int D, const double* G, double* geoF, int recf) {
+// Places G (d xi / dx) at the head of each element's geometry record and the
+// element's mean flow and time-step scale after the face entries.
+__global__ void k_place_elem(SetupDev s, const double* G, double* geoF, int recf) {
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= E) return;
+  if (e >= s.E) return;
+  const int D = s.dim;
   for (int k = 0; k < D * D; ++k) geoF[e * recf + k] = G[e * D * D + k];
+  const int off = D * D + s.nf * (D + 1);
+  const double* v0 = elem_v0(s, e);
+  for (int d = 0; d < D; ++d) geoF[e * recf + off + d] = v0[d];
+  geoF[e * recf + off + D] = s.escale ? s.escale[e] : 1.0;
 }
 
 __global__ void k_to_f32(const double* src, int64_t n, float* dst) {
@@ -368,7 +379,7 @@ inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 namespace dgc {
 
-int run_setup(dg_ctx* c, const dg_mesh_desc* mesh) {
+int run_setup(dg_ctx* c, const dg_mesh_desc* mesh, const double* elem_v0, const double* elem_scale) {
   try {
     Scratch S;
     cudaStream_t st = c->stream;
@@ -406,6 +417,17 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh) {
     for (int d = 0; d < 3; ++d) sd.v0[d] = c->ph.v0[d];
     sd.rho0 = c->ph.rho0, sd.c0 = c->ph.c0;
     sd.ngroups = mesh->n_groups, sd.gbc = gbc, sd.gmask = gmask;
+    sd.ev0 = nullptr, sd.escale = nullptr;
+    if (elem_v0) {
+      double* d = S.alloc<double>(3 * E);
+      SETUP_CK(cudaMemcpyAsync(d, elem_v0, 3 * E * sizeof(double), cudaMemcpyHostToDevice, st));
+      sd.ev0 = d;
+    }
+    if (elem_scale) {
+      double* d = S.alloc<double>(E);
+      SETUP_CK(cudaMemcpyAsync(d, elem_scale, E * sizeof(double), cudaMemcpyHostToDevice, st));
+      sd.escale = d;
+    }
 
     int* err = S.alloc<int>(1);
     SETUP_CK(cudaMemsetAsync(err, 0, sizeof(int), st));
@@ -465,7 +487,7 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh) {
     double* bm64 = S.alloc<double>(nbm);
     SETUP_CK(dev_alloc(c, (void**)&c->d_bcode, (nb > 0 ? nb : 1) * sizeof(int)));
     int* bcode = c->d_bcode;
-    k_place_G<<<blocks(E, 256), 256, 0, st>>>(E, D, G, geo64, recf64);
+    k_place_elem<<<blocks(E, 256), 256, 0, st>>>(sd, G, geo64, recf64);
     k_face_geom<<<blocks(nef, 128), 128, 0, st>>>(sd, det, partner, bidx, geo64, recf64, c->geoI, reci, bm64, bcode,
                                                    err);
     SETUP_CK(cudaGetLastError());
@@ -476,7 +498,7 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh) {
       SETUP_CK(dev_alloc(c, &c->bmat, nbm * sizeof(double)));
       SETUP_CK(cudaMemcpyAsync(c->bmat, bm64, nbm * sizeof(double), cudaMemcpyDeviceToDevice, st));
     } else {
-      const int recf32 = c->sh.recf32, raw = D * D + nf * (D + 1);
+      const int recf32 = c->sh.recf32, raw = D * D + nf * (D + 1) + D + 1;
       SETUP_CK(dev_alloc(c, &c->geoF, Epad * recf32 * sizeof(float)));
       SETUP_CK(cudaMemsetAsync(c->geoF, 0, Epad * recf32 * sizeof(float), st));
       k_geo_to_f32<<<blocks(Epad * raw, 256), 256, 0, st>>>(geo64, recf64, (float*)c->geoF, recf32, Epad, raw);

@@ -80,7 +80,6 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
   for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
   for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
 
-  const T v0x = (T)a.ph.v0[0], v0y = (T)a.ph.v0[1], v0z = (T)a.ph.v0[2];
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
   const int64_t stride = a.stride;
@@ -133,8 +132,9 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
 #pragma unroll
         for (int q = 0; q < NV; ++q) up[q] = ldg(a.y_in + q * stride + (int64_t)nbr * NP + nn);
         const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
-        T vn0 = v0x * n[0] + v0y * n[1];
-        if (D == 3) vn0 += v0z * n[2];
+        const T* ev0 = sGF + e * RECF + S::PHYS_OFF;
+        T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
+        if (D == 3) vn0 += ev0[2] * n[2];
         T avg[NV], dif[NV];
 #pragma unroll
         for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
@@ -179,11 +179,12 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
         }
       }
       const T* G = sGF + e * RECF;
+      const T* ev0 = G + S::PHYS_OFF;
       T gv0[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) {
-        gv0[r] = G[r * D + 0] * v0x + G[r * D + 1] * v0y;
-        if (D == 3) gv0[r] += G[r * D + 2] * v0z;
+        gv0[r] = G[r * D + 0] * ev0[0] + G[r * D + 1] * ev0[1];
+        if (D == 3) gv0[r] += G[r * D + 2] * ev0[2];
       }
 #pragma unroll
       for (int ii = 0; ii < NC; ++ii) {
@@ -218,12 +219,13 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
         for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv * hq[q];
       }
     }
+    const T dte = dt * sGF[e * RECF + S::PHYS_OFF + D];  // dt times the element's step scale
     __syncthreads();  // every thread is done reading sY / sH of this tile
 #pragma unroll
     for (int ii = 0; ii < NC; ++ii)
       if (i0 + ii < NP)
 #pragma unroll
-        for (int q = 0; q < NV; ++q) sY[(q * ET + e) * NPP + i0 + ii] = dt * Lv[ii][q];
+        for (int q = 0; q < NV; ++q) sY[(q * ET + e) * NPP + i0 + ii] = dte * Lv[ii][q];
     __syncthreads();
 
     // ---- stage update over the tile's contiguous DOFs ----

@@ -225,7 +225,6 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
   __syncthreads();
   if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0);
 
-  const T v0x = (T)a.ph.v0[0], v0y = (T)a.ph.v0[1], v0z = (T)a.ph.v0[2];
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
   double red[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -300,11 +299,12 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       for (int r = 0; r < D; ++r)
 #pragma unroll
         for (int d = 0; d < D; ++d) g[r][d] = G[r * D + d];
+      const T* ev0 = G + C::S::PHYS_OFF;
       T gv0[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) {
-        gv0[r] = g[r][0] * v0x + g[r][1] * v0y;
-        if (D == 3) gv0[r] += g[r][2] * v0z;
+        gv0[r] = g[r][0] * ev0[0] + g[r][1] * ev0[1];
+        if (D == 3) gv0[r] += g[r][2] * ev0[2];
       }
 #pragma unroll
       for (int ii = 0; ii < NC; ++ii) {
@@ -359,8 +359,9 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
 #pragma unroll
         for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
         const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
-        T vn0 = v0x * n[0] + v0y * n[1];
-        if (D == 3) vn0 += v0z * n[2];
+        const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
+        T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
+        if (D == 3) vn0 += ev0[2] * n[2];
         T avg[NV], dif[NV];
 #pragma unroll
         for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
@@ -398,6 +399,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     const T* ea = sE + (size_t)NV * ET * NP;
     const T* es = sE + (size_t)2 * NV * ET * NP;
     constexpr int VW = C::VW;
+    const T dte = dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
 #pragma unroll
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
         const int64_t g = q * stride + (e0 + e) * NP + i;
         T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
 #pragma unroll
-        for (int v = 0; v < VW; ++v) kv[v] = dt * Lv[c0 + v][q];
+        for (int v = 0; v < VW; ++v) kv[v] = dte * Lv[c0 + v][q];
         switch (stage) {
           case 0:
             vstore<T, VW>(a.k_out + g, kv);

@@ -19,7 +19,9 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_residuals_noalloc"]
+           "dg_bench_steps", "dg_tune", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
+           "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
+           "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench"]
 
 
 class MeshDesc(C.Structure):
@@ -230,3 +232,125 @@ class Solver:
         self._ck(lib().dg_bench_steps(self.h, n_steps, dt, flush_bytes, C.byref(sm),
                                       C.byref(km) if kernel_time else None), "dg_bench_steps")
         return sm.value, (km.value if kernel_time else None)
+
+
+def _batch_lib():
+    L = lib()
+    if getattr(L, "_batch", False):
+        return L
+    P, D, I64 = C.POINTER, C.c_double, C.c_int64
+    L.dg_batch_create.argtypes = [C.c_int, P(MeshDesc), P(Phys), P(D), C.c_int, C.c_int, P(C.c_void_p)]
+    L.dg_batch_destroy.argtypes = [C.c_void_p]
+    L.dg_batch_last_error.argtypes = [C.c_void_p]
+    L.dg_batch_last_error.restype = C.c_char_p
+    L.dg_batch_info.argtypes = [C.c_void_p, P(C.c_int), P(I64)]
+    L.dg_batch_set_state.argtypes = [C.c_void_p, C.c_int, P(D)]
+    L.dg_batch_get_state.argtypes = [C.c_void_p, C.c_int, P(D)]
+    L.dg_batch_set_sources.argtypes = [C.c_void_p, C.c_int, C.c_int, P(I64), P(I64), I64, P(D)]
+    L.dg_batch_set_observers.argtypes = [C.c_void_p, C.c_int, C.c_int, P(I64), P(I64), P(D)]
+    L.dg_batch_run.argtypes = [C.c_void_p, I64, P(D)]
+    L.dg_batch_bench.argtypes = [C.c_void_p, I64, P(D)]
+    L._batch = True
+    return L
+
+
+class Batch:
+    """A batched ensemble of independent instances (dg_batch_* in the ABI).
+
+    instances: list of dict(mesh=<mesh dict>, v0=(..), dt=float); rho0 and c0
+    are shared by the batch."""
+
+    def __init__(self, instances, rho0=1.0, c0=1.0, precision=DG_FP64, device=0):
+        L = _batch_lib()
+        n = len(instances)
+        descs = (MeshDesc * n)()
+        phys = (Phys * n)()
+        dts = (C.c_double * n)()
+        self._keep = []
+        self.sizes = []
+        for i, inst in enumerate(instances):
+            mesh = inst["mesh"]
+            xyz = np.ascontiguousarray(mesh["xyz"], dtype=np.float64)
+            en = np.ascontiguousarray(mesh["elem_nodes"], dtype=np.int64)
+            groups = mesh.get("groups", [])
+            gbc = np.array([g[0] for g in groups] or [0], dtype=np.int32)
+            goff, gn = _csr([g[1] for g in groups])
+            self._keep += [xyz, en, gbc, goff, gn]
+            d = descs[i]
+            d.dim, d.order, d.nodes_per_elem = mesh["dim"], mesh["order"], en.shape[1]
+            d.n_nodes, d.xyz = xyz.shape[0], _dp(xyz)
+            d.n_elems, d.elem_nodes = en.shape[0], _ip(en)
+            d.n_groups, d.group_bc = len(groups), gbc.ctypes.data_as(C.POINTER(C.c_int))
+            d.group_offsets, d.group_nodes = _ip(goff), _ip(gn)
+            phys[i].v0 = (C.c_double * 3)(*inst.get("v0", (0.0, 0.0, 0.0)))
+            phys[i].rho0, phys[i].c0 = rho0, c0
+            dts[i] = inst["dt"]
+            self.sizes.append((en.shape[0], en.shape[1]))
+        h = C.c_void_p()
+        rc = L.dg_batch_create(n, descs, phys, dts, precision, device, C.byref(h))
+        if rc != 0:
+            raise SolverError("dg_batch_create: %s: %s" % (ERRORS.get(rc, rc), L.dg_last_error(None).decode()))
+        self.h = h
+        self._keep = []
+        self.n = n
+        self.n_obs = [0] * n
+
+    def close(self):
+        if getattr(self, "h", None):
+            _batch_lib().dg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise SolverError("%s: %s: %s" % (what, ERRORS.get(rc, rc),
+                                              _batch_lib().dg_batch_last_error(self.h).decode()))
+
+    def info(self):
+        ng, td = C.c_int(), C.c_int64()
+        self._ck(_batch_lib().dg_batch_info(self.h, C.byref(ng), C.byref(td)), "dg_batch_info")
+        return dict(n_groups=ng.value, total_dofs=td.value)
+
+    def set_state(self, i, u):
+        E, npe = self.sizes[i]
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(4, E * npe)
+        self._ck(_batch_lib().dg_batch_set_state(self.h, i, _dp(u)), "dg_batch_set_state")
+
+    def get_state(self, i):
+        E, npe = self.sizes[i]
+        u = np.zeros((4, E * npe))
+        self._ck(_batch_lib().dg_batch_get_state(self.h, i, _dp(u)), "dg_batch_get_state")
+        return u
+
+    def set_sources(self, i, dof_lists, values):
+        off, flat = _csr(dof_lists)
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1, max(len(dof_lists), 1))
+        self._ck(_batch_lib().dg_batch_set_sources(self.h, i, len(dof_lists), _ip(off), _ip(flat), v.shape[0],
+                                                   _dp(v)), "dg_batch_set_sources")
+
+    def set_observers(self, i, dof_lists, weight_lists):
+        off, flat = _csr(dof_lists)
+        _, w = _csr(weight_lists, np.float64)
+        self._ck(_batch_lib().dg_batch_set_observers(self.h, i, len(dof_lists), _ip(off), _ip(flat), _dp(w)),
+                 "dg_batch_set_observers")
+        self.n_obs[i] = len(dof_lists)
+
+    def run(self, n_steps):
+        tot = sum(n_steps * k * 4 for k in self.n_obs)
+        buf = np.zeros(max(tot, 1))
+        self._ck(_batch_lib().dg_batch_run(self.h, n_steps, _dp(buf)), "dg_batch_run")
+        out, pos = [], 0
+        for k in self.n_obs:
+            out.append(buf[pos:pos + n_steps * k * 4].reshape(n_steps, k, 4))
+            pos += n_steps * k * 4
+        return out
+
+    def bench(self, n_steps):
+        ms = C.c_double()
+        self._ck(_batch_lib().dg_batch_bench(self.h, n_steps, C.byref(ms)), "dg_batch_bench")
+        return ms.value

@@ -170,6 +170,33 @@ int dg_bench_steps(dg_ctx* ctx, int64_t n_steps, double dt, int64_t flush_bytes,
 int dg_residuals_noalloc(const void* u, const void* snap, int precision, int n_var, int64_t n_per_var,
                          int64_t var_stride, double c0, double* res, void* stream);
 
+/* ---- batched ensembles --------------------------------------------------
+ * No counterpart in the reference (one case per process): n independent
+ * instances (own mesh, order, mean flow, sources, observers and time step;
+ * shared rho0 and c0) advanced together. Instances of one element type are
+ * solved as one disjoint-union mesh; each step is one CUDA graph with one
+ * branch per element type. Instances of one element type must have the same
+ * boundary group structure (same number of groups, same BC per group).
+ * dofs below are instance-local (e*Np + n, mesh local node order). */
+typedef struct dg_batch dg_batch;
+int dg_batch_create(int n, const dg_mesh_desc* meshes, const dg_phys* phys, const double* dt, int precision,
+                    int device, dg_batch** out);
+int dg_batch_destroy(dg_batch* b);
+const char* dg_batch_last_error(const dg_batch* b);
+int dg_batch_info(const dg_batch* b, int* n_groups, int64_t* total_dofs);
+int dg_batch_set_state(dg_batch* b, int inst, const double* u);
+int dg_batch_get_state(dg_batch* b, int inst, double* u);
+/* values[step][src] for the instance's global steps [0, n_steps); NaN = inactive */
+int dg_batch_set_sources(dg_batch* b, int inst, int n_src, const int64_t* offsets, const int64_t* dofs,
+                         int64_t n_steps, const double* values);
+int dg_batch_set_observers(dg_batch* b, int inst, int n_obs, const int64_t* offsets, const int64_t* dofs,
+                           const double* weights);
+/* n_steps RK4 steps of every instance (each with its own dt); obs receives,
+ * instance after instance, [n_steps][n_obs_i][4] (p, vx, vy, vz) */
+int dg_batch_run(dg_batch* b, int64_t n_steps, double* obs);
+/* timed steps (CUDA events around each per-step graph launch) */
+int dg_batch_bench(dg_batch* b, int64_t n_steps, double* step_ms);
+
 #ifdef __cplusplus
 }
 #endif
