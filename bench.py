@@ -124,6 +124,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def geometry_record_words(dim, w):
+    """Words of one element's geometry record as the stage kernel reads it:
+    metric (dim*dim), per face normal (dim) and scale, the element's mean flow
+    (dim) and time-step scale, padded to 16 bytes."""
+    raw = dim * dim + (dim + 1) * (dim + 1) + dim + 1
+    vec = 16 // w
+    return (raw + vec - 1) // vec * vec
+
+
 def measured_peak_gbs():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -189,7 +198,7 @@ def run_gpu(args, rank, world):
     # launches (18 state words per DOF incl. the residual snapshot read, plus
     # the per-element geometry records read once per stage) / their time
     w = 4 if args.precision == "fp32" else 8
-    recf = 28 if args.precision == "fp32" else 26
+    recf = geometry_record_words(3, w)
     geo_bytes = 4 * E * (recf * w + 8 * 4)
     alg_bytes = 18 * dofs * w + geo_bytes
     peak, peak_kind = measured_peak_gbs()
