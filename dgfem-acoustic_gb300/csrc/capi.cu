@@ -211,6 +211,10 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   a.dt = dt;
   a.c0sq = c->c0sq;
   a.ph = c->ph;
+  if (c->variant == dgk::kTcVariant) {
+    if constexpr (sizeof(T) == 4) return dgk::launch_stage_tc(c->dim, c->order, a, c->grid2, c->d_err, c->stream);
+    return cudaErrorInvalidValue;
+  }
   if (c->variant >= 0) {
     if constexpr (sizeof(T) == 4)
       return c->dim == 2 ? dgk::launch_stage2_f32_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
@@ -363,11 +367,14 @@ void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>&
 
 
 dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
+  if (v == dgk::kTcVariant)
+    return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order) : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (c->prec == DG_FP32) return c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v) : dgk::stage2_info_f32_3d(c->order, v);
   return c->dim == 2 ? dgk::stage2_info_f64_2d(c->order, v) : dgk::stage2_info_f64_3d(c->order, v);
 }
 
-// Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k.
+// Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
+// kTcVariant the tensor-core kernel (FP32).
 bool set_variant(dg_ctx* c, int v) {
   if (v < 0) {
     c->variant = -1;
@@ -395,6 +402,10 @@ int select_variant(dg_ctx* c, int want) {
     dgk::Stage2Info si = stage2_info(c, v);
     if (si.nc == 0) break;
     if (si.blocks_per_sm > 0) cands.push_back(v);
+  }
+  {
+    dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
+    if (si.nc > 0 && si.blocks_per_sm > 0) cands.push_back(dgk::kTcVariant);
   }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -620,6 +631,11 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     dgk::Stage2Info si = stage2_info(c, v);
     if (si.nc == 0) break;
     c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
+  }
+  {
+    dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
+    if (si.nc > 0)
+      c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
   }
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->partials, c->max_grid * 5 * sizeof(double));
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_err, sizeof(int));

@@ -106,6 +106,11 @@ Stage2Info stage2_info_f32_2d(int order, int variant);
 Stage2Info stage2_info_f32_3d(int order, int variant);
 Stage2Info stage2_info_f64_2d(int order, int variant);
 Stage2Info stage2_info_f64_3d(int order, int variant);
+// Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant id
+// kTcVariant of the context's kernel selection.
+constexpr int kTcVariant = 16;
+cudaError_t launch_stage_tc(int dim, int order, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
+Stage2Info stage_tc_info(int dim, int order);
 // element padding: every tile size divides this
 constexpr int kElemAlign = 128;
 

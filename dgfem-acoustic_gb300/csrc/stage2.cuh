@@ -128,11 +128,101 @@ struct RoundUp {
   static constexpr int v = (N + A - 1) / A * A;
 };
 
+// Per-tile helpers shared by the pipelined and the tensor-core stage kernels.
+// C provides the element shape (D, NP, NF, NFP, NV, NPERM, NK), the tile
+// (ET elements, NT threads), the record sizes and the face-plane stride NKP.
+// Tile buffers: sY [NV][ET][NP], sGF [ET][RECF], sGI [ET][RECI],
+// sN [NV][ET][NKP].
+
+// Issues cp.async gathers of the neighbour traces of every interior face
+// node of the tile into sN (the caller commits and waits).
+template <class C, typename T>
+__device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_t stride, const int* sGI,
+                                              const short* sNb, T* sN, int tid) {
+  constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
+  constexpr int ET = C::ET, NT = C::NT, RECI = C::RECI;
+  for (int q8 = tid; q8 < ET * NK; q8 += NT) {
+    const int el = q8 / NK, k = q8 - el * NK;
+    const int f = k / NFP, m = k - f * NFP;
+    const int code = sGI[el * RECI + NF + f];
+    if (!(code & kCodeBoundary)) {
+      const int nbr = sGI[el * RECI + f];
+      const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
+      const T* src = y_in + (int64_t)nbr * NP + nn;
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        T* dst = sN + (size_t)(q * ET + el) * C::NKP + k;
+        if (sizeof(T) == 4)
+          cp_async4(dst, src + q * stride);
+        else
+          cp_async8(dst, src + q * stride);
+      }
+    }
+  }
+}
+
+// Face numerical fluxes of every face node of the tile, scaled by the face
+// scale sJ, written in place of the gathered traces in sN: the interior
+// Lax-Friedrichs flux (src/Mesh.cpp:761-813) or the boundary matrix
+// (absorbing RKR / reflecting, src/Mesh.cpp:882-972).
+template <class C, typename T>
+__device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T* sY, const T* sGF, const int* sGI,
+                                            const short* sFm, T* sN, int tid, T rhoc2, T inv_rho0, T half_c0) {
+  constexpr int D = C::D, NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NK = C::NK;
+  constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
+  for (int q8 = tid; q8 < ET * NK; q8 += NT) {
+    const int el = q8 / NK, k = q8 - el * NK;
+    const int f = k / NFP;
+    const int node = sFm[k];
+    T um[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) um[q] = sY[(q * ET + el) * NP + node];
+    const int nbr = sGI[el * RECI + f];
+    const int code = sGI[el * RECI + NF + f];
+    const T* gf = sGF + el * RECF + D * D + f * (D + 1);
+    T n[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d) n[d] = gf[d];
+    const T sJ = gf[D];
+    T* slot = sN + (size_t)el * C::NKP + k;  // variable q at slot[q * ET * NKP]
+    T h[NV];
+    if (code & kCodeBoundary) {
+      const T* B = bmat + (int64_t)nbr * NV * NV;
+#pragma unroll
+      for (int q = 0; q < NV; ++q) {
+        T acc = 0;
+#pragma unroll
+        for (int qq = 0; qq < NV; ++qq) acc += __ldg(B + q * NV + qq) * um[qq];
+        h[q] = acc;
+      }
+    } else {
+      T up[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
+      const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
+      const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
+      T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
+      if (D == 3) vn0 += ev0[2] * n[2];
+      T avg[NV], dif[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
+      T nv = n[0] * avg[1] + n[1] * avg[2];
+      if (D == 3) nv += n[2] * avg[3];
+      h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
+#pragma unroll
+      for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) slot[(size_t)q * ET * C::NKP] = sJ * h[q];
+  }
+}
+
 // Compile-time configuration: element shape (D, P), precision T, nodes per
 // thread NC and elements per tile ET.
-template <typename T, int D, int P, int NC_, int ET_>
+template <typename T, int D_, int P, int NC_, int ET_>
 struct Pipe {
-  using S = ShapeT<D, P, T>;
+  using S = ShapeT<D_, P, T>;
+  static constexpr int D = D_;
   static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NV = S::NV, NPERM = S::NPERM, NK = NF * NFP;
   static constexpr int NC = NC_;
   static constexpr int NSPLIT = (NP + NC - 1) / NC;
@@ -247,24 +337,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       if (nepi > 0) issue_epi(tile);
     }
     // ---- neighbour traces: asynchronous gathers into sN ----
-    for (int q8 = tid; q8 < ET * NK; q8 += NT) {
-      const int el = q8 / NK, k = q8 - el * NK;
-      const int f = k / NFP, m = k - f * NFP;
-      const int code = sGI[el * RECI + NF + f];
-      if (!(code & kCodeBoundary)) {
-        const int nbr = sGI[el * RECI + f];
-        const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
-        const T* src = a.y_in + (int64_t)nbr * NP + nn;
-#pragma unroll
-        for (int q = 0; q < NV; ++q) {
-          T* dst = sN + (size_t)(q * ET + el) * C::NKP + k;
-          if (sizeof(T) == 4)
-            cp_async4(dst, src + q * stride);
-          else
-            cp_async8(dst, src + q * stride);
-        }
-      }
-    }
+    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid);
     cp_async_commit();
 
     // ---- volume term for this thread's nodes ----
@@ -329,51 +402,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     __syncthreads();
 
     // ---- face numerical fluxes (in place of the gathered traces) ----
-    for (int q8 = tid; q8 < ET * NK; q8 += NT) {
-      const int el = q8 / NK, k = q8 - el * NK;
-      const int f = k / NFP;
-      const int node = sFm[k];
-      T um[NV];
-#pragma unroll
-      for (int q = 0; q < NV; ++q) um[q] = sY[(q * ET + el) * NP + node];
-      const int nbr = sGI[el * RECI + f];
-      const int code = sGI[el * RECI + NF + f];
-      const T* gf = sGF + el * RECF + D * D + f * (D + 1);
-      T n[3];
-#pragma unroll
-      for (int d = 0; d < D; ++d) n[d] = gf[d];
-      const T sJ = gf[D];
-      T* slot = sN + (size_t)el * C::NKP + k;  // variable q at slot[q * ET * NKP]
-      T h[NV];
-      if (code & kCodeBoundary) {
-        const T* B = a.bmat + (int64_t)nbr * NV * NV;
-#pragma unroll
-        for (int q = 0; q < NV; ++q) {
-          T acc = 0;
-#pragma unroll
-          for (int qq = 0; qq < NV; ++qq) acc += __ldg(B + q * NV + qq) * um[qq];
-          h[q] = acc;
-        }
-      } else {
-        T up[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
-        const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
-        const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
-        T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
-        if (D == 3) vn0 += ev0[2] * n[2];
-        T avg[NV], dif[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
-        T nv = n[0] * avg[1] + n[1] * avg[2];
-        if (D == 3) nv += n[2] * avg[3];
-        h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
-#pragma unroll
-        for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
-      }
-#pragma unroll
-      for (int q = 0; q < NV; ++q) slot[(size_t)q * ET * C::NKP] = sJ * h[q];
-    }
+    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sN, tid, rhoc2, inv_rho0, half_c0);
     __syncthreads();
 
     // ---- lifting ----

@@ -1,0 +1,565 @@
+// Tensor-core fused RK4 stage kernel (sm_103a, FP32 state, tcgen05 3xTF32).
+//
+// Same arithmetic as the reference's per-stage work (src/Mesh.cpp:734-975,
+// src/solver.cpp:38-57, :488-516), written as one small GEMM per tile of
+// ET elements. The RHS of variable q of element e is linear in two sets of
+// per-element values: the contravariant volume fluxes
+//   A_vol[(q,e)][(r,j)] = sum_d G_rd F_{q,d}(y_j)   (r = reference direction)
+// and the scaled face fluxes
+//   A_face[(q,e)][k]    = sJ_f h_q(k)               (k = face node)
+// so that
+//   L[(q,e)][i] = sum_{r,j} Dt_r[i][j] A_vol + sum_k (-LIFT[k][i]) A_face,
+// i.e. D = A B^T with rows m = (q,e) (M = 128), K = (r,j) then k, N = i.
+//
+// Per tile:
+//   * TMA bulk copies land the tile (stage input, geometry records) in a
+//     double buffer, and the RK operands (u, accumulator, snapshot) in a third
+//     buffer, as in the pipelined kernel; neighbour traces are gathered with
+//     cp.async and turned into face fluxes in shared memory;
+//   * each thread owns one row (q,e): it computes the row's A entries, splits
+//     each into a TF32 head and an FP32 tail (x = hi + lo) and writes both to
+//     tensor memory (tcgen05.st), so A never occupies shared memory;
+//   * one thread issues the MMAs D = A_lo B_hi + A_hi B_lo + A_hi B_hi
+//     (tcgen05.mma kind::tf32, A from tensor memory, B = [Dt_1..Dt_D | -LIFT]
+//     split the same way and kept in shared memory in the canonical K-major
+//     no-swizzle layout), completion signalled on an mbarrier;
+//   * the epilogue reads the row's accumulator (tcgen05.ld), applies the RK
+//     update in shared memory and writes the tile back with TMA bulk stores.
+// The split keeps about 21 mantissa bits per product (FP32-level results).
+// Every wait is bounded; on timeout the block records an error flag, waits
+// (bounded) for its own tensor-core work and copies, frees its tensor memory
+// and returns.
+#pragma once
+#include <cstdint>
+
+#include "stage2.cuh"
+
+namespace dgk {
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// tcgen05 shared-memory matrix descriptor: canonical K-major layout without
+// swizzle, made of 8-row x 16-byte core matrices; lbo = byte distance between
+// core matrices adjacent along K, sbo = along M/N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version (tcgen05)
+  return d;
+}
+
+// D[tmem] (+)= A[tmem] * B[smem]^T, kind::tf32, FP32 accumulate.
+__device__ __forceinline__ void umma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                             uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_st4(uint32_t ta, const uint32_t* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(ta), "r"(v[0]), "r"(v[1]),
+               "r"(v[2]), "r"(v[3])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld4(uint32_t ta, float* v) {
+  uint32_t r0, r1, r2, r3;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(ta)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  v[0] = __uint_as_float(r0), v[1] = __uint_as_float(r1), v[2] = __uint_as_float(r2), v[3] = __uint_as_float(r3);
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// 1-D TMA bulk store shared -> global (bytes % 16 == 0, 16-byte aligned).
+__device__ __forceinline__ void tma_store_1d(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Splits four values into TF32 heads and FP32 tails.
+__device__ __forceinline__ void split4(const float* x, uint32_t* hi, uint32_t* lo) {
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    hi[u] = tf32_rna(x[u]);
+    lo[u] = __float_as_uint(x[u] - __uint_as_float(hi[u]));
+  }
+}
+
+template <int N, int A>
+struct RoundUpTc {
+  static constexpr int v = (N + A - 1) / A * A;
+};
+
+template <int X>
+struct Pow2Cols {  // tensor-memory allocation: a power of two >= 32 columns
+  static constexpr int v = X <= 32 ? 32 : X <= 64 ? 64 : X <= 128 ? 128 : X <= 256 ? 256 : 512;
+};
+
+template <int D_, int P>
+struct TcCfg {
+  using T = float;
+  using S = ShapeT<D_, P, float>;
+  static constexpr int D = D_;
+  static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NV = S::NV, NPERM = S::NPERM, NK = NF * NFP;
+  static constexpr int ET = 32;            // elements per tile
+  static constexpr int ROWS = NV * ET;     // used rows of the M = 128 tile
+  static constexpr int NT = 256;           // two threads per row (lane quarters x halves)
+  static constexpr int RECF = S::RECF, RECI = S::RECI;
+  static constexpr int NKP = NK | 1;
+  static constexpr int NPP = RoundUpTc<NP, 4>::v;       // volume block width per direction
+  static constexpr int KV = D * NPP;                     // volume columns
+  static constexpr int KF = RoundUpTc<NK, 4>::v;         // face columns
+  static constexpr int KT = RoundUpTc<KV + KF, 8>::v;    // K (multiple of the TF32 MMA depth 8)
+  static constexpr int NN = RoundUpTc<NP, 16>::v;        // N (multiple of 16 for M = 128)
+  static constexpr int COL_D = 0, COL_AH = NN, COL_AL = NN + KT;  // tensor-memory columns
+  static constexpr int TCOLS = Pow2Cols<NN + 2 * KT>::v;
+  static constexpr int GT = D * D + D + 1;               // per-element values of the row phase
+  static constexpr int VWY = (NP % 4 == 0) ? 4 : (NP % 2 == 0) ? 2 : 1;
+  static constexpr uint32_t YSEG = ET * NP * sizeof(float);
+  static constexpr uint32_t GFB = ET * RECF * sizeof(float);
+  static constexpr uint32_t GIB = ET * RECI * sizeof(int);
+  static constexpr uint32_t BBYTES = NN * KT * 4;        // one operand copy (hi or lo)
+  static constexpr uint32_t LBO = (NN / 8) * 128, SBO = 128;
+  // shared memory layout (bytes)
+  static constexpr size_t oBar = 0;                        // 5 mbarriers + tensor-memory address
+  static constexpr size_t oBh = 128;                       // B hi, canonical layout
+  static constexpr size_t oBl = oBh + BBYTES;              // B lo
+  static constexpr size_t oFm = RoundUpTc<oBl + BBYTES, 16>::v;
+  static constexpr size_t oNb = oFm + RoundUpTc<NK * 2, 16>::v;
+  static constexpr size_t oGT = RoundUpTc<oNb + NF * NPERM * NFP * 2, 16>::v;  // [GT][ET+1]
+  static constexpr size_t oY = RoundUpTc<oGT + GT * (ET + 1) * 4, 128>::v;    // 2 x [NV][ET][NP]
+  static constexpr size_t oGF = oY + 2 * (size_t)NV * YSEG;
+  static constexpr size_t oGI = oGF + 2 * (size_t)GFB;
+  static constexpr size_t oE = RoundUpTc<oGI + 2 * (size_t)GIB, 128>::v;    // [3][NV][ET][NP]
+  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                   // [NV][ET][NKP]
+  static constexpr size_t oR = RoundUpTc<oN + (size_t)NV * ET * NKP * 4, 16>::v;  // [NT/32][5] double
+  static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
+  static_assert(ROWS <= 128, "rows of a tile exceed the MMA height");
+  static_assert(NN + 2 * KT <= 512, "tensor-memory columns exceed the SM's 512");
+  static_assert(YSEG % 16 == 0, "tile segments must be 16-byte multiples");
+  static_assert(bytes <= 227 * 1024, "shared memory of one block exceeds 227 KB");
+};
+
+template <int D, int P>
+__global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageArgs<float> a, int* err) {
+  using C = TcCfg<D, P>;
+  using T = float;
+  constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
+  constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, NPP = C::NPP, KV = C::KV, KF = C::KF, KT = C::KT;
+  constexpr int NN = C::NN, GT = C::GT;
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::oBar);  // 0,1: tile buffers, 2: RK operands, 3: MMA
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::oBar + 64);
+  unsigned char* sBh = sm + C::oBh;
+  unsigned char* sBl = sm + C::oBl;
+  short* sFm = reinterpret_cast<short*>(sm + C::oFm);
+  short* sNb = reinterpret_cast<short*>(sm + C::oNb);
+  T* sGT = reinterpret_cast<T*>(sm + C::oGT);
+  T* sYb = reinterpret_cast<T*>(sm + C::oY);
+  T* sGFb = reinterpret_cast<T*>(sm + C::oGF);
+  int* sGIb = reinterpret_cast<int*>(sm + C::oGI);
+  T* sE = reinterpret_cast<T*>(sm + C::oE);
+  T* sN = reinterpret_cast<T*>(sm + C::oN);
+  double* sRed = reinterpret_cast<double*>(sm + C::oR);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int lq = warp & 3, half = warp >> 2;  // tensor-memory lane quarter, column half
+  const int m = lq * 32 + lane;               // tile row = (q, e)
+  const bool row_ok = lq * 32 < C::ROWS;      // warp-uniform
+  const int q = m / ET, e = m - (m / ET) * ET;
+  const int stage = a.stage;
+  const int64_t stride = a.stride;
+  const int nepi = (stage == 2 || stage == 3) ? 2 : (stage == 4 ? 3 : 0);
+
+  auto issue_tile = [&](int tile, int b) {
+    const int64_t e0 = (int64_t)tile * ET;
+    mbar_expect_tx(&bar[b], NV * C::YSEG + C::GFB + C::GIB);
+#pragma unroll
+    for (int qq = 0; qq < NV; ++qq)
+      tma_load_1d(sYb + ((size_t)b * NV + qq) * ET * NP, a.y_in + qq * stride + e0 * NP, C::YSEG, &bar[b]);
+    tma_load_1d(sGFb + (size_t)b * ET * RECF, a.geoF + e0 * RECF, C::GFB, &bar[b]);
+    tma_load_1d(sGIb + (size_t)b * ET * C::RECI, a.geoI + e0 * C::RECI, C::GIB, &bar[b]);
+  };
+  auto issue_epi = [&](int tile) {
+    const int64_t e0 = (int64_t)tile * ET;
+    mbar_expect_tx(&bar[2], nepi * NV * C::YSEG);
+    for (int k = 0; k < nepi; ++k) {
+      const T* src = k == 0 ? a.u : (k == 1 ? a.acc : a.snap);
+#pragma unroll
+      for (int qq = 0; qq < NV; ++qq)
+        tma_load_1d(sE + ((size_t)k * NV + qq) * ET * NP, src + qq * stride + e0 * NP, C::YSEG, &bar[2]);
+    }
+  };
+
+  // ---- setup: barriers, tensor memory, operator B (hi/lo), node tables ----
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i) mbar_init(&bar[i], 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"((uint32_t)C::TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int idx = tid; idx < NN * KT; idx += NT) {
+    const int n = idx / KT, k = idx - (idx / KT) * KT;
+    float x = 0.f;
+    if (n < NP) {
+      if (k < KV) {
+        const int r = k / NPP, j = k - (k / NPP) * NPP;
+        if (j < NP) x = a.Dt[(r * NP + j) * NP + n];
+      } else if (k - KV < NK) {
+        x = -a.LIFT[(k - KV) * NP + n];
+      }
+    }
+    const uint32_t off = (uint32_t)((k / 4) * (NN / 8) + n / 8) * 128 + (n % 8) * 16 + (k % 4) * 4;
+    const uint32_t h = tf32_rna(x);
+    *reinterpret_cast<uint32_t*>(sBh + off) = h;
+    *reinterpret_cast<float*>(sBl + off) = x - __uint_as_float(h);
+  }
+  for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
+  for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B is read by the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t trow = tbase + ((uint32_t)(lq * 32) << 16);
+  // A columns that no tile writes are zero: padding past KV + KF, and every
+  // column of the rows past ROWS
+  {
+    const uint32_t z[4] = {0u, 0u, 0u, 0u};
+    if (row_ok) {
+      for (int c = KV + KF + 4 * half; c < KT; c += 8) {
+        tmem_st4(trow + C::COL_AH + c, z);
+        tmem_st4(trow + C::COL_AL + c, z);
+      }
+    } else {
+      for (int c = 4 * half; c < KT; c += 8) {
+        tmem_st4(trow + C::COL_AH + c, z);
+        tmem_st4(trow + C::COL_AL + c, z);
+      }
+    }
+    tmem_wait_st();
+  }
+
+  const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
+  const T dt = (T)a.dt;
+  double red_a = 0.0, red_b = 0.0;  // this row's residual sums: (snap-u)^2, and for p also in density units
+  bool ok = true;
+  // thread 0: barriers whose armed phase was not yet observed complete (bit i)
+  // and that phase's parity (bit 4+i); drained before the block exits
+  uint32_t pend = 0;
+  auto arm = [&](int i, int parity) { pend = (pend & ~(0x11u << i)) | (1u << i) | ((uint32_t)(parity & 1) << (4 + i)); };
+  auto seen = [&](int i) { pend &= ~(1u << i); };
+  if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0), arm(0, 0);
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+
+  int it = 0;
+  for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    const int64_t e0 = (int64_t)tile * ET;
+    bool got = mbar_wait(&bar[b], (it >> 1) & 1);
+    if (tid == 0 && got) seen(b);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    T* sY = sYb + (size_t)b * NV * ET * NP;
+    const T* sGF = sGFb + (size_t)b * ET * RECF;
+    const int* sGI = sGIb + (size_t)b * ET * C::RECI;
+    if (tid == 0) {
+      fence_proxy_async();
+      const int nt = tile + gridDim.x;
+      if (nt < a.ntiles) issue_tile(nt, b ^ 1), arm(b ^ 1, (it + 1) >> 1);
+      bulk_wait_read();  // the previous tile's stores have read the operand buffer
+      if (nepi > 0) issue_epi(tile), arm(2, it);
+    }
+    // ---- neighbour traces (asynchronous) ----
+    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid);
+    cp_async_commit();
+    // ---- per-element values of the row phase, element-minor ----
+    for (int w = tid; w < ET * GT; w += NT) {
+      const int el = w / GT, v = w - (w / GT) * GT;
+      const int src = v < D * D ? v : C::S::PHYS_OFF + (v - D * D);
+      sGT[v * (ET + 1) + el] = sGF[el * RECF + src];
+    }
+    __syncthreads();
+
+    // ---- volume rows: A_vol[(q,e)][(r,j)] -> tensor memory ----
+    T g[D][D], gv0[D];
+    if (row_ok) {
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[r][d] = sGT[(r * D + d) * (ET + 1) + e];
+      T v0[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) v0[d] = sGT[(D * D + d) * (ET + 1) + e];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        gv0[r] = g[r][0] * v0[0] + g[r][1] * v0[1];
+        if (D == 3) gv0[r] += g[r][2] * v0[2];
+      }
+      const T* ye = sY + e * NP;
+      for (int g4 = half; g4 < NPP / 4; g4 += 2) {
+        const int j0 = g4 * 4;
+        T yp[4], yv[D][4];
+        // p and the velocity components this row needs (all of them for the p row)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int j = j0 + jj < NP ? j0 + jj : NP - 1;
+          yp[jj] = ye[j];
+#pragma unroll
+          for (int d = 0; d < D; ++d) yv[d][jj] = (q == 0 || q == 1 + d) ? ye[(1 + d) * ET * NP + j] : (T)0;
+        }
+        T fr[D][4];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+#pragma unroll
+          for (int r = 0; r < D; ++r) {
+            T x;
+            if (q == 0) {
+              T gw = g[r][0] * yv[0][jj] + g[r][1] * yv[1][jj];
+              if (D == 3) gw += g[r][2] * yv[2][jj];
+              x = gv0[r] * yp[jj] + rhoc2 * gw;
+            } else {
+              const int dq = q - 1;
+              T gr = g[r][0];
+              T vq = yv[0][jj];
+#pragma unroll
+              for (int d = 1; d < D; ++d)
+                if (dq == d) gr = g[r][d], vq = yv[d][jj];
+              x = gv0[r] * vq + gr * yp[jj] * inv_rho0;
+            }
+            fr[r][jj] = (j0 + jj < NP) ? x : (T)0;
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          uint32_t hi[4], lo[4];
+          split4(fr[r], hi, lo);
+          tmem_st4(trow + C::COL_AH + r * NPP + j0, hi);
+          tmem_st4(trow + C::COL_AL + r * NPP + j0, lo);
+        }
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- face numerical fluxes (in place of the gathered traces) ----
+    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sN, tid, rhoc2, inv_rho0, half_c0);
+    __syncthreads();
+
+    // ---- face rows: A_face[(q,e)][k] -> tensor memory ----
+    if (row_ok) {
+      const T* hrow = sN + (size_t)(q * ET + e) * C::NKP;
+      for (int c4 = half; c4 < KF / 4; c4 += 2) {
+        T x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = (c4 * 4 + u < NK) ? hrow[c4 * 4 + u] : (T)0;
+        uint32_t hi[4], lo[4];
+        split4(x, hi, lo);
+        tmem_st4(trow + C::COL_AH + KV + c4 * 4, hi);
+        tmem_st4(trow + C::COL_AL + KV + c4 * 4, lo);
+      }
+    }
+    tmem_wait_st();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+
+    // ---- D = A_lo B_hi + A_hi B_lo + A_hi B_hi ----
+    if (tid == 0) {
+      const uint32_t bh = smem_u32(sBh), bl = smem_u32(sBl);
+#pragma unroll 1
+      for (int pass = 0; pass < 3; ++pass) {
+        const uint32_t acol = pass == 0 ? C::COL_AL : C::COL_AH;
+        const uint32_t bsrc = pass == 1 ? bl : bh;
+#pragma unroll 1
+        for (int ks = 0; ks < KT / 8; ++ks)
+          umma_tf32_ts(tbase + C::COL_D, tbase + acol + ks * 8, umma_desc(bsrc + ks * 2 * C::LBO, C::LBO, C::SBO),
+                       idesc, (pass > 0 || ks > 0) ? 1u : 0u);
+      }
+      umma_commit(&bar[3]);
+      arm(3, it);
+    }
+    got = mbar_wait(&bar[3], it & 1);
+    if (tid == 0 && got) seen(3);
+    if (nepi > 0 && got) {
+      got = mbar_wait(&bar[2], it & 1);
+      if (tid == 0 && got) seen(2);
+    }
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+
+    // ---- epilogue: RK update of this row's nodes in the operand buffer ----
+    if (row_ok) {
+      const T dte = dt * sGT[(D * D + D) * (ET + 1) + e];
+      T* s0 = sE;
+      T* s1 = sE + (size_t)NV * ET * NP;
+      const T* s2 = sE + (size_t)2 * NV * ET * NP;
+      const int rb = (q * ET + e) * NP;
+      for (int c4 = half; c4 < NN / 4; c4 += 2) {
+        if (c4 * 4 >= NP) break;  // warp-uniform
+        float dv[4];
+        tmem_ld4(trow + C::COL_D + c4 * 4, dv);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = c4 * 4 + u;
+          if (i >= NP) break;
+          const T kv = dte * dv[u];
+          const int l = rb + i;
+          switch (stage) {
+            case 0:
+              s0[l] = kv;
+              break;
+            case 1: {
+              const T xu = sY[l];
+              s0[l] = kv;
+              s1[l] = xu + (T)0.5 * kv;
+              break;
+            }
+            case 2:
+            case 3: {
+              const T xu = s0[l], xa = s1[l];
+              s1[l] = xa + (T)2 * kv;
+              s0[l] = xu + (stage == 2 ? (T)0.5 * kv : kv);
+              break;
+            }
+            case 4: {
+              const T xu = s0[l], xa = s1[l], xs = s2[l];
+              const T un = xu + (xa + kv) / (T)6;
+              s0[l] = un;
+              const double sn = (double)xs, dn = sn - (double)un;
+              red_a += dn * dn;
+              if (q == 0) {
+                const double dr = sn / a.c0sq - (double)un / a.c0sq;
+                red_b += dr * dr;
+              }
+              break;
+            }
+            default: {
+              const T xu = sY[l];
+              s0[l] = xu + kv;
+              break;
+            }
+          }
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the bulk stores read these values
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      // outputs per stage: (slot, destination)
+      T* dst0 = nullptr;
+      T* dst1 = nullptr;
+      switch (stage) {
+        case 0: dst0 = a.k_out; break;
+        case 1: dst0 = a.acc, dst1 = a.y_out; break;
+        case 2:
+        case 3: dst0 = a.y_out, dst1 = a.acc; break;
+        case 4: dst0 = a.u; break;
+        default: dst0 = a.y_out; break;
+      }
+#pragma unroll
+      for (int qq = 0; qq < NV; ++qq) {
+        tma_store_1d(dst0 + qq * stride + e0 * NP, sE + (size_t)qq * ET * NP, C::YSEG);
+        if (dst1) tma_store_1d(dst1 + qq * stride + e0 * NP, sE + ((size_t)NV + qq) * ET * NP, C::YSEG);
+      }
+      bulk_commit();
+    }
+  }
+
+  // ---- teardown: own copies and tensor-core work first, then the memory ----
+  if (tid == 0) {
+    bulk_wait_all();
+    // after a timeout: bounded waits for the copies and the MMA group still
+    // armed, so that nothing lands in freed shared or tensor memory
+    for (int i = 0; i < 4; ++i)
+      if (pend & (1u << i)) mbar_wait(&bar[i], (pend >> (4 + i)) & 1u);
+  }
+  if (!ok && tid == 0) atomicOr(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"((uint32_t)C::TCOLS)
+                 : "memory");
+
+  if (stage == 4) {
+    // residual components: 0 p, 1 p/c0^2, 2.. velocity components
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      double v = !row_ok ? 0.0 : (c == 0 ? (q == 0 ? red_a : 0.0) : c == 1 ? red_b : (q == c - 1 ? red_a : 0.0));
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if (lane == 0) sRed[warp * 5 + c] = v;
+    }
+    __syncthreads();
+    if (tid < 5) {
+      double v = 0.0;
+      for (int w = 0; w < NT / 32; ++w) v += sRed[w * 5 + tid];
+      a.partials[blockIdx.x * 5 + tid] = v;
+    }
+  }
+}
+
+template <int D, int P>
+struct StageTc {
+  using C = TcCfg<D, P>;
+  static int blocks_per_sm() {
+    auto kfn = stage_tc_kernel<D, P>;
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, C::NT, C::bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    // resident blocks of one SM share its 512 tensor-memory columns
+    const int by_tmem = 512 / C::TCOLS;
+    return nb < by_tmem ? nb : by_tmem;
+  }
+  static cudaError_t launch(const StageArgs<float>& a, int grid, int* err, cudaStream_t s) {
+    auto kfn = stage_tc_kernel<D, P>;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    kfn<<<grid, C::NT, C::bytes, s>>>(a, err);
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace dgk

@@ -89,7 +89,7 @@ typedef struct {
   int64_t penalty_sign_hist[2]; /* interior faces with s_f = -1, +1 */
   int64_t device_bytes;
   double setup_ms;
-  int kernel_variant; /* stage kernel in use: -1 baseline, k >= 0 pipelined variant k */
+  int kernel_variant; /* stage kernel in use: -1 baseline, 0..15 pipelined variant k, 16 tensor-core kernel */
 } dg_info_t;
 
 int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out);
@@ -132,8 +132,10 @@ int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
  * keep the fastest (what dg_create does; the environment variable
  * DGFEM_STAGE_VARIANT overrides it there); -1: baseline kernel; k >= 0:
  * pipelined variant k (TMA-staged tiles; the variants differ in output nodes
- * per thread and elements per tile). Returns DG_ERR_ARG for a variant that
- * does not exist for this element type. */
+ * per thread and elements per tile); 16: tensor-core kernel (FP32 contexts
+ * only: tcgen05 MMAs with a 3xTF32 split, FP32-level results). Returns
+ * DG_ERR_ARG for a variant that does not exist for this element type or
+ * precision. */
 int dg_tune(dg_ctx* ctx, int variant);
 
 /* The CUDA stream (cudaStream_t) all work of ctx is issued on. */
