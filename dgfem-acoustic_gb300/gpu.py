@@ -21,7 +21,10 @@ SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_st
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
            "dg_bench_steps", "dg_tune", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
-           "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench"]
+           "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench",
+           "dg_mlp_create", "dg_mlp_destroy", "dg_mlp_last_error", "dg_mlp_param_count", "dg_mlp_set_params",
+           "dg_mlp_get_params", "dg_mlp_forward", "dg_mlp_forward_device", "dg_mlp_gradient", "dg_mlp_set_data",
+           "dg_mlp_train"]
 
 
 class MeshDesc(C.Structure):
@@ -354,3 +357,101 @@ class Batch:
         ms = C.c_double()
         self._ck(_batch_lib().dg_batch_bench(self.h, n_steps, C.byref(ms)), "dg_batch_bench")
         return ms.value
+
+
+def _mlp_lib():
+    L = lib()
+    if getattr(L, "_mlp", False):
+        return L
+    P, D, I64, F = C.POINTER, C.c_double, C.c_int64, C.c_float
+    L.dg_mlp_create.argtypes = [C.c_int, P(C.c_int), C.c_int, P(C.c_void_p)]
+    L.dg_mlp_destroy.argtypes = [C.c_void_p]
+    L.dg_mlp_last_error.argtypes = [C.c_void_p]
+    L.dg_mlp_last_error.restype = C.c_char_p
+    L.dg_mlp_param_count.argtypes = [C.c_void_p]
+    L.dg_mlp_param_count.restype = I64
+    L.dg_mlp_set_params.argtypes = [C.c_void_p, P(F)]
+    L.dg_mlp_get_params.argtypes = [C.c_void_p, P(F)]
+    L.dg_mlp_forward.argtypes = [C.c_void_p, P(F), I64, P(F)]
+    L.dg_mlp_forward_device.argtypes = [C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p]
+    L.dg_mlp_gradient.argtypes = [C.c_void_p, P(F), P(F), I64, P(F), P(D)]
+    L.dg_mlp_set_data.argtypes = [C.c_void_p, P(F), P(F), I64]
+    L.dg_mlp_train.argtypes = [C.c_void_p, I64, C.c_int, D, D, C.c_uint64, P(D)]
+    L._mlp = True
+    return L
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Network:
+    """Fully connected GELU network on the GPU (dg_mlp_* in the ABI).
+
+    widths: [inputs, hidden..., outputs]. Parameters are one flat float32
+    vector, per layer W [out][in] (row-major) then b [out]."""
+
+    def __init__(self, widths, device=0):
+        L = _mlp_lib()
+        w = (C.c_int * len(widths))(*widths)
+        h = C.c_void_p()
+        rc = L.dg_mlp_create(len(widths) - 1, w, device, C.byref(h))
+        if rc != 0:
+            raise SolverError("dg_mlp_create: %s: %s" % (ERRORS.get(rc, rc), L.dg_mlp_last_error(None).decode()))
+        self.h = h
+        self.widths = list(widths)
+        self.n_params = L.dg_mlp_param_count(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            _mlp_lib().dg_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise SolverError("%s: %s: %s" % (what, ERRORS.get(rc, rc), _mlp_lib().dg_mlp_last_error(self.h).decode()))
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        if p.size != self.n_params:
+            raise ValueError("expected %d parameters, got %d" % (self.n_params, p.size))
+        self._ck(_mlp_lib().dg_mlp_set_params(self.h, _fp(p)), "dg_mlp_set_params")
+
+    def get_params(self):
+        p = np.zeros(self.n_params, dtype=np.float32)
+        self._ck(_mlp_lib().dg_mlp_get_params(self.h, _fp(p)), "dg_mlp_get_params")
+        return p
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.widths[0])
+        y = np.zeros((x.shape[0], self.widths[-1]), dtype=np.float32)
+        self._ck(_mlp_lib().dg_mlp_forward(self.h, _fp(x), x.shape[0], _fp(y)), "dg_mlp_forward")
+        return y
+
+    def forward_device(self, x_ptr, n, y_ptr, stream=None):
+        self._ck(_mlp_lib().dg_mlp_forward_device(self.h, x_ptr, n, y_ptr, stream), "dg_mlp_forward_device")
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.widths[0])
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(x.shape[0], self.widths[-1])
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_double()
+        self._ck(_mlp_lib().dg_mlp_gradient(self.h, _fp(x), _fp(t), x.shape[0], _fp(g), C.byref(loss)),
+                 "dg_mlp_gradient")
+        return g, loss.value
+
+    def set_data(self, x, t):
+        self._x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.widths[0])
+        self._t = np.ascontiguousarray(t, dtype=np.float32).reshape(self._x.shape[0], self.widths[-1])
+        self._ck(_mlp_lib().dg_mlp_set_data(self.h, _fp(self._x), _fp(self._t), self._x.shape[0]), "dg_mlp_set_data")
+
+    def train(self, n_steps, batch, lr, lr_final, seed=0):
+        losses = np.zeros(max(n_steps, 1))
+        self._ck(_mlp_lib().dg_mlp_train(self.h, n_steps, batch, lr, lr_final, seed, _dp(losses)), "dg_mlp_train")
+        return losses[:n_steps]

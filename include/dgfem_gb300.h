@@ -199,6 +199,38 @@ int dg_batch_run(dg_batch* b, int64_t n_steps, double* obs);
 /* timed steps (CUDA events around each per-step graph launch) */
 int dg_batch_bench(dg_batch* b, int64_t n_steps, double* step_ms);
 
+/* ------------------------------------------------------------------------
+ * Learned spectral surrogate (no counterpart in the reference, which answers
+ * every parameter query with a DG run; DG stays the fallback and the judge
+ * of the surrogate's error). A fully connected network: widths[0] inputs,
+ * n_layers - 1 GELU hidden layers, a linear output layer of widths[n_layers];
+ * BF16 weights in the forward/backward passes, FP32 master weights, FP32
+ * accumulation. Parameters are one flat FP32 vector, layer after layer:
+ * W_l [widths[l+1]][widths[l]] (row-major) then b_l [widths[l+1]].
+ * ------------------------------------------------------------------------ */
+typedef struct dg_mlp dg_mlp;
+int dg_mlp_create(int n_layers, const int* widths, int device, dg_mlp** out);
+int dg_mlp_destroy(dg_mlp* m);
+const char* dg_mlp_last_error(dg_mlp* m);
+int64_t dg_mlp_param_count(dg_mlp* m);
+/* host FP32 parameters in/out; setting them resets the optimiser state */
+int dg_mlp_set_params(dg_mlp* m, const float* params);
+int dg_mlp_get_params(dg_mlp* m, float* params);
+/* n rows of inputs [n][widths[0]] -> outputs [n][widths[n_layers]]: host
+ * arrays (synchronous), or device arrays on the given CUDA stream (NULL: the
+ * network's own stream; asynchronous) */
+int dg_mlp_forward(dg_mlp* m, const float* x, int64_t n, float* y);
+int dg_mlp_forward_device(dg_mlp* m, const float* x, int64_t n, float* y, void* stream);
+/* gradient of the mean squared error over the n x widths[n_layers] outputs
+ * against targets t, written as one flat vector like the parameters */
+int dg_mlp_gradient(dg_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss);
+/* training rows (host arrays, copied to the device once) */
+int dg_mlp_set_data(dg_mlp* m, const float* x, const float* t, int64_t n);
+/* n_steps Adam steps (beta 0.9/0.999, eps 1e-8) on shuffled mini-batches
+ * (one permutation per epoch from seed), learning rate decaying from lr to
+ * lr_final on a cosine; losses (optional) receives each step's batch loss */
+int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, uint64_t seed, double* losses);
+
 #ifdef __cplusplus
 }
 #endif

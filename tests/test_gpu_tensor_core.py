@@ -18,6 +18,14 @@ pytestmark = pytest.mark.gpu
 TC = 16
 
 
+def _obs_err(tr, ref_obs):
+    """Relative L2 over the observer samples; an observer with no DG node in
+    its radius reports NaN (the reference's rule) in both."""
+    ok = np.isfinite(ref_obs)
+    assert np.array_equal(np.isfinite(tr), ok)
+    return rel_l2(tr[ok], ref_obs[ok])
+
+
 def _solver(pkg, mesh, ph, prec="fp32"):
     return pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
 
@@ -90,7 +98,7 @@ def test_tc_run_matches_oracle(pkg, oracle, dim, p):
     nv = dim + 1
     assert rel_l2(u[:nv], ref["state"][:nv]) <= 1e-5
     assert rel_l2(res[:, :4], ref["residuals"][:, :4]) <= 1e-3
-    assert rel_l2(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= 1e-4
+    assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= 1e-4
 
 
 @pytest.mark.parametrize("prec,variant", [("fp64", -1), ("fp64", 0), ("fp32", 1), ("fp32", TC)])
@@ -102,7 +110,7 @@ def test_euler_run_matches_oracle(pkg, oracle, dim, p, prec, variant):
     nv = dim + 1
     tol = 1e-12 if prec == "fp64" else 1e-5
     assert rel_l2(u[:nv], ref["state"][:nv]) <= tol
-    assert rel_l2(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= tol * 10
+    assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= tol * 10
 
 
 def test_tc_many_tiles_per_block(pkg, oracle):
