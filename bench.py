@@ -228,40 +228,7 @@ def run_gpu(args, rank, world):
     return line
 
 
-ENSEMBLE = dict(name="batched ensemble: 256 2-D LEE instances, 1k-50k tris, p in {2,3,4}", n=256, seed=4,
-                half_width=5.0, rho0=1.225, c0=340.0, cfl=0.5, jitter=0.2,
-                observers=[(2.5, 2.5, 0.0, 0.3), (-2.5, 2.5, 0.0, 0.3), (-2.5, -2.5, 0.0, 0.3), (2.5, -2.5, 0.0, 0.3)])
-
-
-def ensemble_instances(n=None, seed=None):
-    """Seeded draws of the ensemble workload: element count log-uniform in
-    [1e3, 5e4] (grid n = ceil(sqrt(E/2))), order uniform in {2,3,4}, monopole
-    position uniform in [-4,4]^2, frequency uniform in [20,400] Hz, Mach
-    uniform in [0,0.3] in a uniform direction, all sides Absorbing, dt from
-    CFL 0.5."""
-    pkg = _pkg()
-    W = ENSEMBLE
-    n = n or W["n"]
-    rng = np.random.default_rng(W["seed"] if seed is None else seed)
-    out = []
-    for k in range(n):
-        E = float(np.exp(rng.uniform(np.log(1e3), np.log(5e4))))
-        grid = int(np.ceil(np.sqrt(E / 2)))
-        p = int(rng.integers(2, 5))
-        sx, sy = rng.uniform(-4, 4, 2)
-        f = rng.uniform(20, 400)
-        M = rng.uniform(0, 0.3)
-        th = rng.uniform(0, 2 * np.pi)
-        v0 = (M * W["c0"] * np.cos(th), M * W["c0"] * np.sin(th), 0.0)
-        m = pkg.meshgen.square(n=grid, order=p, half_width=W["half_width"], jitter=W["jitter"],
-                               seed=int(rng.integers(1 << 30)))
-        mesh = dict(dim=2, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"],
-                    groups=pkg.meshgen.solver_groups(m, {"Absorbing": "Absorbing"}))
-        h = 2 * W["half_width"] / grid * (1 - 2 * W["jitter"])
-        dt = W["cfl"] * h / ((W["c0"] + np.linalg.norm(v0)) * (2 * p + 1))
-        src = [sx, sy, 0.0, 0.2, 0.1, f, 0.0, 1e9]
-        out.append(dict(mesh=mesh, v0=v0, dt=dt, src=src, obs=W["observers"], p=p))
-    return out
+ENSEMBLE_NAME = "batched ensemble: 256 2-D LEE instances, 1k-50k tris, p in {2,3,4}"
 
 
 def run_ensemble(args):
@@ -269,21 +236,13 @@ def run_ensemble(args):
     plain single-instance path on a sample of the same instances, and the
     per-instance FP32 error against the FP64 batch."""
     pkg = _pkg()
+    ens = pkg.ensemble
     t0 = time.perf_counter()
-    insts = ensemble_instances()
+    insts = ens.draw_instances(256, seed=4)
     gen_s = time.perf_counter() - t0
-    W = ENSEMBLE
 
     def make(prec, subset):
-        B = pkg.gpu.Batch([dict(mesh=i["mesh"], v0=i["v0"], dt=i["dt"]) for i in subset], rho0=W["rho0"],
-                          c0=W["c0"], precision=prec)
-        for k, i in enumerate(subset):
-            sd, od, ow = node_sets(i["mesh"], i["src"], i["obs"])
-            n = args.warmup + args.steps + 2
-            t = np.arange(n) * i["dt"]
-            B.set_sources(k, sd, (i["src"][4] * np.sin(2 * np.pi * i["src"][5] * t))[:, None])
-            B.set_observers(k, od, ow)
-        return B
+        return ens.make_batch(subset, prec, args.warmup + args.steps + 2)
 
     dofs = sum(i["mesh"]["elem_nodes"].size * 3 for i in insts)
     B = make(pkg.gpu.DG_FP32, insts)
@@ -296,7 +255,7 @@ def run_ensemble(args):
     sample = insts[::32]
     tot_dof, tot_ms = 0, 0.0
     for i in sample:
-        S = pkg.gpu.Solver(i["mesh"], v0=i["v0"], rho0=W["rho0"], c0=W["c0"], precision=pkg.gpu.DG_FP32)
+        S = pkg.gpu.Solver(i["mesh"], v0=i["v0"], rho0=ens.RHO0, c0=ens.C0, precision=pkg.gpu.DG_FP32)
         sd, od, ow = node_sets(i["mesh"], i["src"], i["obs"])
         S.set_sources(sd)
         t = np.arange(args.warmup + 3 * args.steps + 8) * i["dt"]
@@ -326,7 +285,7 @@ def run_ensemble(args):
     errs = [float(np.linalg.norm(a[:3] - b[:3]) / np.linalg.norm(b[:3])) for a, b in zip(res[1], res[0])]
     return {"metric": "RK4 DOF-updates/s (batched ensemble)", "value": batched, "unit": UNIT,
             "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
-            "config": {"workload": W["name"], "instances": len(insts), "dofs": int(dofs),
+            "config": {"workload": ENSEMBLE_NAME, "instances": len(insts), "dofs": int(dofs),
                        "elements": int(sum(i["mesh"]["elem_nodes"].shape[0] for i in insts)),
                        "orders": {str(p): sum(1 for i in insts if i["p"] == p) for p in (2, 3, 4)},
                        "generation_s": gen_s},
@@ -335,6 +294,46 @@ def run_ensemble(args):
             "batched_over_plain": batched / plain,
             "fp32_vs_fp64_rel_l2_max": max(errs), "error_steps": nerr, "error_instances": len(sub),
             "clocks": clk.summary()}
+
+
+SURROGATE_PATH = os.path.join(ROOT, "dgfem-acoustic_gb300", "data", "surrogate.npz")
+
+
+def run_surrogate(args, n_dg=256, bound_db=1.0):
+    """The learned spectral surrogate against DG: query throughput of the
+    surrogate (both networks, host arrays in and out) on the 2,000 held-out
+    parameter draws, the batched DG path's query throughput on the first
+    n_dg of them (same mesh and step count the targets came from), and the
+    surrogate's spectral error against those DG answers."""
+    pkg = _pkg()
+    S = pkg.surrogate
+    if not os.path.exists(SURROGATE_PATH):
+        return {"metric": "surrogate spectral queries/s", "unavailable": "no trained surrogate at %s" % SURROGATE_PATH}
+    sur = S.Surrogate.load(SURROGATE_PATH)
+    P = S.draw_params(2000, 6)
+    Y, dg_s = S.dg_spectra(P[:n_dg], steps=sur.steps, grid=sur.grid)
+    for _ in range(args.warmup):
+        sur.predict(P)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sur.predict(P)
+    q_s = len(P) * args.steps / (time.perf_counter() - t0)
+    mean, est = sur.predict(P[:n_dg])
+    err = S.rms_db(mean, Y)
+    acc = est <= bound_db
+    spec, from_dg, _ = sur.query(P[:n_dg], bound_db=bound_db)
+    delivered = S.rms_db(spec, Y)
+    return {"metric": "surrogate spectral queries/s", "value": q_s, "unit": "queries/s", "steps": args.steps,
+            "warmup": args.warmup, "dtype": "bf16 weights, f32 accumulate",
+            "config": {"workload": "learned surrogate: 6 -> 4x256 GELU -> 4x128 log-PSD, 2 networks",
+                       "queries": len(P), "dg_grid": sur.grid, "dg_steps": sur.steps},
+            "dg": {"value": n_dg / dg_s, "unit": "queries/s", "sample": "%d held-out draws, batched FP32 DG" % n_dg},
+            "speedup_over_dg": q_s / (n_dg / dg_s),
+            "heldout": {"queries": n_dg, "bound_db": bound_db, "rms_db_median": float(np.median(err)),
+                        "rms_db_p95": float(np.quantile(err, 0.95)), "accepted_fraction": float(acc.mean()),
+                        "accepted_rms_db_max": float(err[acc].max()) if acc.any() else None,
+                        "delivered_rms_db_max": float(delivered.max()),
+                        "rerun_through_dg": int(from_dg.sum())}}
 
 
 def run_profile(args):
@@ -406,7 +405,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=-2,
                     help="stage kernel variant (-2: autotuned at setup, -1: baseline kernel, k: pipelined variant k)")
-    ap.add_argument("--workload", default="cube", choices=["cube", "ensemble"])
+    ap.add_argument("--workload", default="cube", choices=["cube", "ensemble", "surrogate"])
     ap.add_argument("--profile", action="store_true",
                     help="only build the workload and run warmup + steps time steps (for ncu captures)")
     args = ap.parse_args()
@@ -422,6 +421,10 @@ def main():
     if args.workload == "ensemble" and args.impl != "reference":
         if rank == 0:
             print(json.dumps(run_ensemble(args)), flush=True)
+        return
+    if args.workload == "surrogate" and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps(run_surrogate(args)), flush=True)
         return
     if args.impl == "reference":
         if rank == 0:

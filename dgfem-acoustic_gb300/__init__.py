@@ -3,7 +3,8 @@
 A drop-in for the RK4 LEE hot path of DGFEM-Acoustic: host front end
 (host.py, libdgfem_host.so), GPU solver behind a C ABI (gpu.py,
 libdgfem_gb300.so), the dgalerkin driver executable, and mesh generators
-(meshgen.py). Build with build.build() (or __graft_entry__.build()).
+(meshgen.py), the batched-ensemble workload (ensemble.py) and its learned spectral
+surrogate (surrogate.py). Build with build.build() (or __graft_entry__.build()).
 """
 import importlib.util as _ilu
 import os as _os
@@ -22,3 +23,5 @@ build = _load("build")
 host = _load("host")
 gpu = _load("gpu")
 meshgen = _load("meshgen")
+ensemble = _load("ensemble")
+surrogate = _load("surrogate")

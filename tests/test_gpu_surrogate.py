@@ -1,0 +1,93 @@
+"""The learned spectral surrogate against the method without it (DG for every
+query), on a small configuration (10 x 10 grid meshes, 400 RK4 steps, 600
+training runs) so that DG data generation and training take seconds.
+
+What the network gains: it answers queries at >= 100x the rate of the DG
+runs it replaces, it predicts held-out spectra better than the best constant
+guess (the mean training spectrum), and its fallback hands every query whose
+estimated error is above the bound back to DG, whose answers it returns
+unchanged."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GRID, STEPS = 10, 400
+
+
+@pytest.fixture(scope="module")
+def trained(pkg):
+    S = pkg.surrogate
+    P_train = S.draw_params(600, 15)
+    P_test = S.draw_params(48, 16)
+    Y_train, _ = S.dg_spectra(P_train, steps=STEPS, grid=GRID)
+    Y_test, dg_s = S.dg_spectra(P_test, steps=STEPS, grid=GRID)
+    sur = S.Surrogate.fit(P_train[:500], Y_train[:500], steps=1500, batch=100, lr=2e-3, lr_final=2e-5,
+                          grid=GRID, dg_steps=STEPS)
+    sur.calibrate(P_train[500:], Y_train[500:])
+    yield S, sur, P_train, Y_train, P_test, Y_test, dg_s
+    sur.close()
+
+
+def test_targets_are_finite_spectra(trained):
+    S, _, _, Y_train, _, Y_test, _ = trained
+    assert Y_train.shape == (600, S.N_OBS, S.N_BINS)
+    assert np.all(np.isfinite(Y_train)) and np.all(np.isfinite(Y_test))
+    # floored at most the dynamic range below each observer's peak
+    span = Y_train.max(axis=2) - Y_train.min(axis=2)
+    assert np.all(span <= S.DYN_RANGE_DB + 1e-6)
+
+
+def test_surrogate_beats_constant_guess(trained):
+    S, sur, _, Y_train, P_test, Y_test, _ = trained
+    mean, est = sur.predict(P_test)
+    err = S.rms_db(mean, Y_test)
+    base = S.rms_db(np.broadcast_to(Y_train[:500].mean(axis=0), Y_test.shape), Y_test)
+    assert np.median(err) < 0.7 * np.median(base), (np.median(err), np.median(base))
+    assert np.all(est >= 0)
+
+
+def test_surrogate_throughput_over_dg(trained):
+    _, sur, _, _, P_test, _, dg_s = trained
+    sur.predict(P_test)
+    t0 = time.perf_counter()
+    for _ in range(10):
+        sur.predict(P_test)
+    sur_s = (time.perf_counter() - t0) / 10
+    assert dg_s / sur_s >= 100, (dg_s, sur_s)
+
+
+def test_fallback_returns_dg_answers(trained):
+    S, sur, _, _, P_test, Y_test, _ = trained
+    q = P_test[:12]
+    # a bound no estimate meets: every query goes to DG and comes back unchanged
+    spec, from_dg, _ = sur.query(q, bound_db=-1.0)
+    assert from_dg.all()
+    np.testing.assert_allclose(spec, Y_test[:12], rtol=0, atol=1e-9)
+    # an unbounded tolerance: every query is answered by the network
+    spec2, from_dg2, _ = sur.query(q, bound_db=np.inf)
+    assert not from_dg2.any()
+    mean, _ = sur.predict(q)
+    np.testing.assert_array_equal(spec2, mean)
+    # a mixed bound: accepted rows come from the network, the others from DG
+    _, est = sur.predict(q)
+    b = float(np.median(est))
+    spec3, from_dg3, _ = sur.query(q, bound_db=b)
+    assert np.array_equal(from_dg3, est > b)
+    np.testing.assert_allclose(spec3[from_dg3], Y_test[:12][from_dg3], rtol=0, atol=1e-9)
+    np.testing.assert_array_equal(spec3[~from_dg3], mean[~from_dg3])
+
+
+def test_save_load_round_trip(trained, tmp_path):
+    S, sur, _, _, P_test, _, _ = trained
+    path = str(tmp_path / "s.npz")
+    sur.save(path)
+    s2 = S.Surrogate.load(path)
+    a, ea = sur.predict(P_test)
+    b, eb = s2.predict(P_test)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(ea, eb)
+    assert (s2.grid, s2.steps) == (GRID, STEPS)
+    s2.close()
