@@ -55,9 +55,8 @@ def build_problem(counts=None):
     m = pkg.meshgen.box(counts=counts or W["counts"], order=W["order"], jitter=W["jitter"], seed=W["seed"])
     mesh = dict(dim=3, order=W["order"], xyz=m["xyz"], elem_nodes=m["elem_nodes"],
                 groups=pkg.meshgen.solver_groups(m, BCS))
-    # dt = CFL * h_min / ((c0 + |v0|) (2p + 1)), h_min = shortest element edge
-    en, X = m["elem_nodes"][:, :4], m["xyz"]
-    hmin = min(np.linalg.norm(X[en[:, a]] - X[en[:, b]], axis=1).min() for a in range(4) for b in range(a + 1, 4))
+    # dt = CFL * h_min / ((c0 + |v0|) (2p + 1)), h_min = smallest element altitude
+    hmin = pkg.meshgen.min_altitude(mesh)
     dt = W["cfl"] * hmin / ((W["c0"] + np.linalg.norm(W["v0"])) * (2 * W["order"] + 1))
     rng = np.random.default_rng(W["seed"])
     obs = [tuple(rng.uniform(-0.8, 0.8, 3)) + (0.1,) for _ in range(W["n_obs"])]

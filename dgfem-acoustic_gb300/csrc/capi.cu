@@ -661,9 +661,12 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
   c->info.device_bytes = c->device_bytes;
   c->info.setup_ms = ms;
   {
+    // DGFEM_STAGE_VARIANT forces a kernel where it exists for this context
+    // (e.g. the tensor-core kernel only for FP32); elsewhere the autotuner picks
     const char* ev = std::getenv("DGFEM_STAGE_VARIANT");
     int want = ev ? std::atoi(ev) : -2;
     int rc2 = select_variant(c, want);
+    if (rc2 == DG_ERR_ARG && ev) rc2 = select_variant(c, -2);
     if (rc2 != DG_OK) {
       std::string m = c->err;
       dg_destroy(c);

@@ -116,6 +116,41 @@ struct Pow2Cols {  // tensor-memory allocation: a power of two >= 32 columns
   static constexpr int v = X <= 32 ? 32 : X <= 64 ? 64 : X <= 128 ? 128 : X <= 256 ? 256 : 512;
 };
 
+// Four consecutive row entries row[j0 .. j0+3] of a row of NP values in
+// shared memory (row start 4*VW-byte aligned when VW > 1), in VW-wide
+// vectors; entries past NP (the last group of a row whose NP is not a
+// multiple of 4) read into the next row or pad and must be masked by the
+// caller.
+template <int NP, int VW>
+__device__ __forceinline__ void load4(float* v, const float* row, int j0) {
+  if constexpr (VW == 4) {
+    const float4 x = *reinterpret_cast<const float4*>(row + j0);
+    v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w;
+  } else if constexpr (VW == 2) {
+    const float2 x = *reinterpret_cast<const float2*>(row + j0);
+    const float2 y = *reinterpret_cast<const float2*>(row + j0 + 2);
+    v[0] = x.x, v[1] = x.y, v[2] = y.x, v[3] = y.y;
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = row[j0 + u < NP ? j0 + u : NP - 1];
+  }
+}
+
+// Stores the entries of v that fall inside the row (j0 + u < NP).
+template <int NP, int VW>
+__device__ __forceinline__ void store4(float* row, int j0, const float* v) {
+  if constexpr (VW == 4) {
+    *reinterpret_cast<float4*>(row + j0) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (VW == 2) {
+    *reinterpret_cast<float2*>(row + j0) = make_float2(v[0], v[1]);
+    if (j0 + 2 < NP) *reinterpret_cast<float2*>(row + j0 + 2) = make_float2(v[2], v[3]);
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (j0 + u < NP) row[j0 + u] = v[u];
+  }
+}
+
 template <int D_, int P>
 struct TcCfg {
   using T = float;
@@ -139,20 +174,26 @@ struct TcCfg {
   static constexpr uint32_t YSEG = ET * NP * sizeof(float);
   static constexpr uint32_t GFB = ET * RECF * sizeof(float);
   static constexpr uint32_t GIB = ET * RECI * sizeof(int);
-  static constexpr uint32_t BBYTES = NN * KT * 4;        // one operand copy (hi or lo)
-  static constexpr uint32_t LBO = (NN / 8) * 128, SBO = 128;
+  // B is stored with only the 8-row groups that hold nodes (NG of NN/8): the
+  // MMA reads NN rows per K chunk, and the rows past NG*8 run into the next
+  // chunk (or the slack after B lo); they only feed accumulator columns >= NP,
+  // which are never read
+  static constexpr int NG = (NP + 7) / 8;
+  static constexpr uint32_t BBYTES = (KT / 4) * NG * 128;  // one operand copy (hi or lo)
+  static constexpr uint32_t BSLACK = (NN / 8 - NG) * 128;
+  static constexpr uint32_t LBO = NG * 128, SBO = 128;
   // shared memory layout (bytes)
   static constexpr size_t oBar = 0;                        // 5 mbarriers + tensor-memory address
   static constexpr size_t oBh = 128;                       // B hi, canonical layout
   static constexpr size_t oBl = oBh + BBYTES;              // B lo
-  static constexpr size_t oFm = RoundUpTc<oBl + BBYTES, 16>::v;
+  static constexpr size_t oFm = RoundUpTc<oBl + BBYTES + BSLACK, 16>::v;
   static constexpr size_t oNb = oFm + RoundUpTc<NK * 2, 16>::v;
   static constexpr size_t oGT = RoundUpTc<oNb + NF * NPERM * NFP * 2, 16>::v;  // [GT][ET+1]
   static constexpr size_t oY = RoundUpTc<oGT + GT * (ET + 1) * 4, 128>::v;    // 2 x [NV][ET][NP]
   static constexpr size_t oGF = oY + 2 * (size_t)NV * YSEG;
   static constexpr size_t oGI = oGF + 2 * (size_t)GFB;
-  static constexpr size_t oE = RoundUpTc<oGI + 2 * (size_t)GIB, 128>::v;    // [3][NV][ET][NP]
-  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                   // [NV][ET][NKP]
+  static constexpr size_t oE = RoundUpTc<oGI + 2 * (size_t)GIB, 128>::v;    // [2][NV][ET][NP]
+  static constexpr size_t oN = oE + 2 * (size_t)NV * YSEG;                   // [NV][ET][NKP]
   static constexpr size_t oR = RoundUpTc<oN + (size_t)NV * ET * NKP * 4, 16>::v;  // [NT/32][5] double
   static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
   static_assert(ROWS <= 128, "rows of a tile exceed the MMA height");
@@ -190,7 +231,9 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
   const int q = m / ET, e = m - (m / ET) * ET;
   const int stage = a.stage;
   const int64_t stride = a.stride;
-  const int nepi = (stage == 2 || stage == 3) ? 2 : (stage == 4 ? 3 : 0);
+  // RK operands staged by TMA: u and the accumulator (stages 2-4); the
+  // residual snapshot of stage 4 is read straight from global memory
+  const int nepi = (stage >= 2 && stage <= 4) ? 2 : 0;
 
   auto issue_tile = [&](int tile, int b) {
     const int64_t e0 = (int64_t)tile * ET;
@@ -205,7 +248,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
     const int64_t e0 = (int64_t)tile * ET;
     mbar_expect_tx(&bar[2], nepi * NV * C::YSEG);
     for (int k = 0; k < nepi; ++k) {
-      const T* src = k == 0 ? a.u : (k == 1 ? a.acc : a.snap);
+      const T* src = k == 0 ? a.u : a.acc;
 #pragma unroll
       for (int qq = 0; qq < NV; ++qq)
         tma_load_1d(sE + ((size_t)k * NV + qq) * ET * NP, src + qq * stride + e0 * NP, C::YSEG, &bar[2]);
@@ -223,7 +266,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  for (int idx = tid; idx < NN * KT; idx += NT) {
+  for (int idx = tid; idx < C::NG * 8 * KT; idx += NT) {
     const int n = idx / KT, k = idx - (idx / KT) * KT;
     float x = 0.f;
     if (n < NP) {
@@ -234,11 +277,13 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
         x = -a.LIFT[(k - KV) * NP + n];
       }
     }
-    const uint32_t off = (uint32_t)((k / 4) * (NN / 8) + n / 8) * 128 + (n % 8) * 16 + (k % 4) * 4;
+    const uint32_t off = (uint32_t)((k / 4) * C::NG + n / 8) * 128 + (n % 8) * 16 + (k % 4) * 4;
     const uint32_t h = tf32_rna(x);
     *reinterpret_cast<uint32_t*>(sBh + off) = h;
     *reinterpret_cast<float*>(sBl + off) = x - __uint_as_float(h);
   }
+  for (int i = tid; i < (int)(C::BSLACK / 4); i += NT)
+    reinterpret_cast<float*>(sBl + C::BBYTES)[i] = 0.f;
   for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
   for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B is read by the tensor cores
@@ -327,13 +372,16 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
       for (int g4 = half; g4 < NPP / 4; g4 += 2) {
         const int j0 = g4 * 4;
         T yp[4], yv[D][4];
-        // p and the velocity components this row needs (all of them for the p row)
+        // p and the velocity components this row needs (all of them for the
+        // p row); lanes are consecutive elements, so vector loads keep the
+        // NP-word stride free of bank conflicts
+        load4<NP, C::VWY>(yp, ye, j0);
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const int j = j0 + jj < NP ? j0 + jj : NP - 1;
-          yp[jj] = ye[j];
-#pragma unroll
-          for (int d = 0; d < D; ++d) yv[d][jj] = (q == 0 || q == 1 + d) ? ye[(1 + d) * ET * NP + j] : (T)0;
+        for (int d = 0; d < D; ++d) {
+          if (q == 0 || q == 1 + d)
+            load4<NP, C::VWY>(yv[d], ye + (1 + d) * ET * NP, j0);
+          else
+            yv[d][0] = yv[d][1] = yv[d][2] = yv[d][3] = (T)0;
         }
         T fr[D][4];
 #pragma unroll
@@ -420,56 +468,64 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
 
     // ---- epilogue: RK update of this row's nodes in the operand buffer ----
     if (row_ok) {
+      constexpr int VW = C::VWY;
       const T dte = dt * sGT[(D * D + D) * (ET + 1) + e];
-      T* s0 = sE;
-      T* s1 = sE + (size_t)NV * ET * NP;
-      const T* s2 = sE + (size_t)2 * NV * ET * NP;
-      const int rb = (q * ET + e) * NP;
+      T* r0 = sE + (size_t)(q * ET + e) * NP;                  // slot 0 row: u in, new y or u out
+      T* r1 = sE + (size_t)(NV * ET + q * ET + e) * NP;        // slot 1 row: acc in, new acc out
+      const T* ry = sY + (size_t)(q * ET + e) * NP;            // stage input row (u in stages 1, 5)
+      const T* gs = a.snap + q * stride + (e0 + e) * NP;      // residual snapshot row (stage 4)
       for (int c4 = half; c4 < NN / 4; c4 += 2) {
-        if (c4 * 4 >= NP) break;  // warp-uniform
+        const int i0 = c4 * 4;
+        if (i0 >= NP) break;  // warp-uniform
         float dv[4];
-        tmem_ld4(trow + C::COL_D + c4 * 4, dv);
+        tmem_ld4(trow + C::COL_D + i0, dv);
+        T kv[4], x0[4], x1[4], o0[4], o1[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int i = c4 * 4 + u;
-          if (i >= NP) break;
-          const T kv = dte * dv[u];
-          const int l = rb + i;
-          switch (stage) {
-            case 0:
-              s0[l] = kv;
-              break;
-            case 1: {
-              const T xu = sY[l];
-              s0[l] = kv;
-              s1[l] = xu + (T)0.5 * kv;
-              break;
-            }
-            case 2:
-            case 3: {
-              const T xu = s0[l], xa = s1[l];
-              s1[l] = xa + (T)2 * kv;
-              s0[l] = xu + (stage == 2 ? (T)0.5 * kv : kv);
-              break;
-            }
-            case 4: {
-              const T xu = s0[l], xa = s1[l], xs = s2[l];
-              const T un = xu + (xa + kv) / (T)6;
-              s0[l] = un;
-              const double sn = (double)xs, dn = sn - (double)un;
-              red_a += dn * dn;
-              if (q == 0) {
-                const double dr = sn / a.c0sq - (double)un / a.c0sq;
-                red_b += dr * dr;
+        for (int u = 0; u < 4; ++u) kv[u] = dte * dv[u];
+        switch (stage) {
+          case 0:
+            store4<NP, VW>(r0, i0, kv);
+            break;
+          case 1:
+            load4<NP, VW>(x0, ry, i0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) o1[u] = x0[u] + (T)0.5 * kv[u];
+            store4<NP, VW>(r0, i0, kv);
+            store4<NP, VW>(r1, i0, o1);
+            break;
+          case 2:
+          case 3:
+            load4<NP, VW>(x0, r0, i0);
+            load4<NP, VW>(x1, r1, i0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              o1[u] = x1[u] + (T)2 * kv[u], o0[u] = x0[u] + (stage == 2 ? (T)0.5 * kv[u] : kv[u]);
+            store4<NP, VW>(r1, i0, o1);
+            store4<NP, VW>(r0, i0, o0);
+            break;
+          case 4:
+            load4<NP, VW>(x0, r0, i0);
+            load4<NP, VW>(x1, r1, i0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              o0[u] = x0[u] + (x1[u] + kv[u]) / (T)6;
+              if (i0 + u < NP) {
+                const double sn = (double)gs[i0 + u], dn = sn - (double)o0[u];
+                red_a += dn * dn;
+                if (q == 0) {
+                  const double dr = sn / a.c0sq - (double)o0[u] / a.c0sq;
+                  red_b += dr * dr;
+                }
               }
-              break;
             }
-            default: {
-              const T xu = sY[l];
-              s0[l] = xu + kv;
-              break;
-            }
-          }
+            store4<NP, VW>(r0, i0, o0);
+            break;
+          default:
+            load4<NP, VW>(x0, ry, i0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) o0[u] = x0[u] + kv[u];
+            store4<NP, VW>(r0, i0, o0);
+            break;
         }
       }
     }

@@ -8,7 +8,8 @@ triangles, n = ceil(sqrt(E/2)), interior vertices jittered by up to 20 % of
 the spacing), order uniform in {2, 3, 4}, monopole position uniform in
 [-4, 4]^2, frequency uniform in [20, 400] Hz, Mach number uniform in
 [0, 0.3] in a uniform direction (v0 = M c0 (cos th, sin th)), all sides
-Absorbing, time step from CFL 0.5: dt = CFL h_min / ((c0 + |v0|)(2p + 1)).
+Absorbing, time step from CFL 0.5: dt = CFL h_min / ((c0 + |v0|)(2p + 1)),
+h_min the smallest element altitude of the instance's mesh.
 """
 import importlib
 import math
@@ -34,15 +35,18 @@ def square_mesh(grid, p, seed):
                 groups=mg.solver_groups(m, {"Absorbing": "Absorbing"}))
 
 
-def time_step(grid, p, mach):
-    h = 2 * HALF_WIDTH / grid * (1 - 2 * JITTER)
-    return CFL * h / ((C0 + mach * C0) * (2 * p + 1))
+def time_step(mesh, p, mach):
+    """dt = CFL h_min / ((c0 + |v0|)(2p + 1)), h_min the mesh's smallest
+    element altitude (cached on the mesh dict)."""
+    if "h_min" not in mesh:
+        mesh["h_min"] = _pkg().meshgen.min_altitude(mesh)
+    return CFL * mesh["h_min"] / ((C0 + mach * C0) * (2 * p + 1))
 
 
-def instance(mesh, grid, p, sx, sy, f, mach, theta):
+def instance(mesh, p, sx, sy, f, mach, theta):
     v0 = (mach * C0 * math.cos(theta), mach * C0 * math.sin(theta), 0.0)
     src = [sx, sy, 0.0, SOURCE_SIZE, SOURCE_AMP, f, 0.0, 1e9]  # x,y,z,size,amp,freq,phase,duration
-    return dict(mesh=mesh, v0=v0, dt=time_step(grid, p, mach), src=src, obs=OBSERVERS, p=p,
+    return dict(mesh=mesh, v0=v0, dt=time_step(mesh, p, mach), src=src, obs=OBSERVERS, p=p,
                 params=(sx, sy, f, mach, theta, p))
 
 
@@ -59,7 +63,7 @@ def draw_instances(n=256, seed=4):
         mach = rng.uniform(0, 0.3)
         th = rng.uniform(0, 2 * np.pi)
         mesh = square_mesh(grid, p, int(rng.integers(1 << 30)))
-        out.append(instance(mesh, grid, p, sx, sy, f, mach, th))
+        out.append(instance(mesh, p, sx, sy, f, mach, th))
     return out
 
 

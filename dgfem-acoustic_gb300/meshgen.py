@@ -217,3 +217,24 @@ def solver_groups(mesh, bc_by_name):
         if t in ("Absorbing", "Reflecting"):
             out.append((1 if t == "Reflecting" else 0, nodes))
     return out
+
+
+def min_altitude(mesh):
+    """Smallest element altitude of a straight-sided simplex mesh: 2 area /
+    longest edge (triangles) or 3 volume / largest face (tetrahedra). This is
+    the h_min of the project's time-step rule dt = CFL h_min / ((c0 + |v0|)
+    (2p + 1)): the shortest distance a wave crosses an element, which bounds
+    the stable explicit step on distorted elements."""
+    X = np.asarray(mesh["xyz"], dtype=np.float64)
+    dim = mesh.get("dim", 3 if X.shape[1] == 3 and np.ptp(X[:, 2]) > 0 else 2)
+    en = np.asarray(mesh["elem_nodes"])[:, :dim + 1]
+    P = [X[en[:, i]] for i in range(dim + 1)]
+    if dim == 2:
+        area = 0.5 * np.abs((P[1][:, 0] - P[0][:, 0]) * (P[2][:, 1] - P[0][:, 1])
+                            - (P[1][:, 1] - P[0][:, 1]) * (P[2][:, 0] - P[0][:, 0]))
+        L = np.max([np.linalg.norm(P[b] - P[a], axis=1) for a, b in ((0, 1), (1, 2), (2, 0))], axis=0)
+        return float((2 * area / L).min())
+    V = np.abs(np.einsum("ij,ij->i", P[1] - P[0], np.cross(P[2] - P[0], P[3] - P[0]))) / 6
+    A = np.max([0.5 * np.linalg.norm(np.cross(P[b] - P[a], P[c] - P[a]), axis=1)
+                for a, b, c in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))], axis=0)
+    return float((3 * V / A).min())

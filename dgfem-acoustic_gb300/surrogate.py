@@ -106,7 +106,7 @@ def dg_spectra(params, chunk=2000, steps=STEPS, grid=GRID, precision=None, progr
     dg_s = 0.0
     for c0 in range(0, P.shape[0], chunk):
         rows = P[c0:c0 + chunk]
-        insts = [ens.instance(meshes[int(r[5])], grid, int(r[5]), r[0], r[1], r[2], r[3], r[4]) for r in rows]
+        insts = [ens.instance(meshes[int(r[5])], int(r[5]), r[0], r[1], r[2], r[3], r[4]) for r in rows]
         B = ens.make_batch(insts, precision, steps)
         traces = [np.zeros((steps, N_OBS)) for _ in insts]
         t0 = time.perf_counter()
