@@ -221,7 +221,7 @@ def run_gpu(args, rank, world):
                      "kernel_ms_per_step": kern_ms, "algorithmic_bytes_per_step": int(alg_bytes)},
         "clocks": clk.summary(),
         "setup_ms": info["setup_ms"],
-        "kernel_variant": info["kernel_variant"],
+        "kernel_variant": info["kernel_variant"], "kernel_grid": info["kernel_grid"],
     }
     S.close()
     return line
@@ -335,6 +335,19 @@ def run_surrogate(args, n_dg=256, bound_db=1.0):
                         "rerun_through_dg": int(from_dg.sum())}}
 
 
+def run_ensemble_profile(args):
+    """Warm-up plus a few steps of the 256-instance ensemble (FP32 batch),
+    nothing else (the command line of the ensemble ncu summaries)."""
+    pkg = _pkg()
+    insts = pkg.ensemble.draw_instances(256, seed=4)
+    B = pkg.ensemble.make_batch(insts, pkg.gpu.DG_FP32, args.warmup + args.steps + 2)
+    B.run(args.warmup)
+    obs = B.run(args.steps)
+    print(json.dumps({"profile": True, "workload": "ensemble", "steps": args.steps, "warmup": args.warmup,
+                      "groups": B.info()["n_groups"], "p_obs0_last": float(obs[0][-1, 0, 0])}))
+    B.close()
+
+
 def run_profile(args):
     """Warm-up plus a few RK4 steps of the workload through the per-step graph,
     nothing else (the command line that the ncu summaries in profiles/ use)."""
@@ -415,7 +428,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     if args.profile:
-        run_profile(args)
+        if args.workload == "ensemble":
+            run_ensemble_profile(args)
+        else:
+            run_profile(args)
         return
     if args.workload == "ensemble" and args.impl != "reference":
         if rank == 0:

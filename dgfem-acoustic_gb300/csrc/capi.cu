@@ -674,6 +674,7 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     }
   }
   c->info.kernel_variant = c->variant;
+  c->info.kernel_grid = c->variant >= 0 ? c->grid2 : c->grid;
   *out = c;
   return DG_OK;
 }
@@ -906,6 +907,7 @@ int dg_tune(dg_ctx* c, int variant) {
   if (!c) return DG_ERR_ARG;
   int rc = select_variant(c, variant);
   c->info.kernel_variant = c->variant;
+  c->info.kernel_grid = c->variant >= 0 ? c->grid2 : c->grid;
   return rc;
 }
 

@@ -521,6 +521,8 @@ struct Stage2 {
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
       configured = true;
     }
@@ -531,7 +533,11 @@ struct Stage2 {
     auto kfn = stage2_kernel<T, D, P, NC_, ET_>;
     // a configuration larger than the shared memory of an SM is reported as
     // unavailable; the failed query must not leave a sticky launch error
-    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) {
+    // the largest shared-memory carve-out, so that the occupancy query and
+    // the launches see the same per-SM capacity
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+            cudaSuccess) {
       cudaGetLastError();
       return 0;
     }

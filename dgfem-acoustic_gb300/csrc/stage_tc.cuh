@@ -592,7 +592,11 @@ struct StageTc {
   using C = TcCfg<D, P>;
   static int blocks_per_sm() {
     auto kfn = stage_tc_kernel<D, P>;
-    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess) {
+    // the largest shared-memory carve-out, so that the occupancy query and
+    // the launches see the same per-SM capacity
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+            cudaSuccess) {
       cudaGetLastError();
       return 0;
     }
@@ -610,6 +614,8 @@ struct StageTc {
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
       configured = true;
     }

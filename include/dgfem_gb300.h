@@ -90,6 +90,7 @@ typedef struct {
   int64_t device_bytes;
   double setup_ms;
   int kernel_variant; /* stage kernel in use: -1 baseline, 0..15 pipelined variant k, 16 tensor-core kernel */
+  int kernel_grid;    /* blocks of each stage-kernel launch (persistent blocks for variants >= 0) */
 } dg_info_t;
 
 int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out);
