@@ -903,6 +903,20 @@ int dg_face_info(dg_ctx* c, int64_t* nbr, int* penalty, int* bc) {
 
 void* dg_stream(dg_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+int dg_kernel_info(dg_ctx* c, int variant, int* out) {
+  if (!c || !out) return fail(c, DG_ERR_ARG, "dg_kernel_info: invalid argument");
+  for (int i = 0; i < 5; ++i) out[i] = 0;
+  if (variant < 0) {
+    out[0] = (int)c->sh.et, out[1] = c->sh.nt, out[4] = c->grid;
+    return DG_OK;
+  }
+  dgk::Stage2Info si = stage2_info(c, variant);
+  if (si.nc == 0) return DG_OK;
+  out[0] = si.et, out[1] = si.nt, out[2] = si.smem_bytes, out[3] = si.blocks_per_sm;
+  out[4] = (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms);
+  return DG_OK;
+}
+
 int dg_tune(dg_ctx* c, int variant) {
   if (!c) return DG_ERR_ARG;
   int rc = select_variant(c, variant);

@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
+           "dg_bench_steps", "dg_tune", "dg_kernel_info", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
            "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench",
            "dg_mlp_create", "dg_mlp_destroy", "dg_mlp_last_error", "dg_mlp_param_count", "dg_mlp_set_params",
@@ -76,6 +76,7 @@ def lib():
         L.dg_stream.restype = C.c_void_p
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
         L.dg_tune.argtypes = [C.c_void_p, C.c_int]
+        L.dg_kernel_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
         L.dg_residuals_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, I64, I64, D, C.c_void_p,
                                            C.c_void_p]
         _lib = L
@@ -222,6 +223,13 @@ class Solver:
         self._ck(lib().dg_face_info(self.h, _ip(nbr), pen.ctypes.data_as(C.POINTER(C.c_int)),
                                     bc.ctypes.data_as(C.POINTER(C.c_int))), "dg_face_info")
         return dict(nbr=nbr.reshape(-1, nf), penalty=pen.reshape(-1, nf), bc=bc.reshape(-1, nf))
+
+    def kernel_info(self, variant):
+        """(elements per tile, threads, shared bytes, blocks per SM, grid) of a
+        stage-kernel variant; elements per tile 0 = not available."""
+        out = (C.c_int * 5)()
+        self._ck(lib().dg_kernel_info(self.h, variant, out), "dg_kernel_info")
+        return tuple(out)
 
     def tune(self, variant=-2):
         self._ck(lib().dg_tune(self.h, variant), "dg_tune")

@@ -14,13 +14,17 @@ bound is re-run through DG. The error estimate is the disagreement of two
 independently trained networks, scaled so that it covers the true error of
 95 % of a calibration split.
 
-Targets: the observer pressure trace of STEPS RK4 steps goes through the
-project's restatement of the reference's PSD_spec (host.spectra: largest
-power-of-two prefix, mean removed, one-sided periodogram,
-src/fft.cpp:183-227); the linear power is averaged over 128 bins of width
-F_MAX/128 (interpolated at the bin centre where a bin holds no FFT line) and
-expressed in dB re (20 uPa)^2, floored DYN_RANGE_DB below each observer's
-peak bin. Instances use one fixed jittered GRID x GRID mesh per order, so the
+Targets: the last power-of-two samples of the observer pressure trace of
+STEPS RK4 steps (the settled part: the first samples hold the wave-front
+arrival), Hann-tapered and power-normalised, go through the project's
+restatement of the reference's PSD_spec (host.spectra: mean removed,
+one-sided periodogram, src/fft.cpp:183-227); the linear power is averaged
+over 128 bins of width F_MAX/128 (interpolated at the bin centre where a bin
+holds no FFT line) and expressed in dB re (20 uPa)^2, floored DYN_RANGE_DB
+below each observer's peak bin. The taper replaces the rectangular window's
+leakage pattern, which oscillates with f times the window length (and so
+with f, p and M) faster than the parameter sampling resolves, by a compact
+main lobe. Instances use one fixed jittered GRID x GRID mesh per order, so the
 spectrum is a function of the six parameters alone.
 """
 import importlib
@@ -69,8 +73,17 @@ def features(params):
 
 
 def log_psd_bins(trace, dt):
-    """128-bin log-PSD (dB re (20 uPa)^2) of one pressure trace."""
-    _, psd = _pkg().host.spectra(np.asarray(trace, dtype=np.float32), dt)
+    """128-bin log-PSD (dB re (20 uPa)^2) of one pressure trace: the last
+    power-of-two samples (the settled part of the run), Hann-tapered and
+    power-normalised, through the PSD_spec restatement."""
+    tr = np.asarray(trace, dtype=np.float64)
+    n = 1
+    while n * 2 <= len(tr):
+        n *= 2
+    seg = tr[len(tr) - n:]
+    w = 0.5 * (1.0 - np.cos(2 * np.pi * np.arange(n) / (n - 1)))
+    seg = (seg - seg.mean()) * w / math.sqrt(np.mean(w * w))
+    _, psd = _pkg().host.spectra(seg.astype(np.float32), dt)
     f, P = psd[:, 0], psd[:, 1]
     edges = np.arange(N_BINS + 1) * (F_MAX / N_BINS)
     idx = np.searchsorted(edges, f, side="right") - 1

@@ -139,6 +139,13 @@ int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
  * precision. */
 int dg_tune(dg_ctx* ctx, int variant);
 
+/* Launch shape of stage-kernel variant `variant` (as in dg_tune) for this
+ * context: out[0] elements per tile (0: not available), out[1] threads per
+ * block, out[2] dynamic shared memory bytes, out[3] resident blocks per SM
+ * (the occupancy query, capped by tensor memory for the tensor-core kernel),
+ * out[4] the grid a launch would use. */
+int dg_kernel_info(dg_ctx* ctx, int variant, int* out);
+
 /* The CUDA stream (cudaStream_t) all work of ctx is issued on. */
 void* dg_stream(dg_ctx* ctx);
 /* Timed RK4 steps for benchmarking: runs n_steps with the per-step graph and
