@@ -215,6 +215,11 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
     if constexpr (sizeof(T) == 4) return dgk::launch_stage_tc(c->dim, c->order, a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
   }
+  if (c->variant >= dgk::kStage3Variant) {
+    if constexpr (sizeof(T) == 4)
+      return dgk::launch_stage3(c->dim, c->order, c->variant - dgk::kStage3Variant, a, c->grid2, c->d_err, c->stream);
+    return cudaErrorInvalidValue;
+  }
   if (c->variant >= 0) {
     if constexpr (sizeof(T) == 4)
       return c->dim == 2 ? dgk::launch_stage2_f32_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
@@ -367,6 +372,9 @@ void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>&
 
 
 dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
+  if (v >= dgk::kStage3Variant)
+    return c->prec == DG_FP32 ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
+                              : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (v == dgk::kTcVariant)
     return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order) : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (c->prec == DG_FP32) return c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v) : dgk::stage2_info_f32_3d(c->order, v);
@@ -374,7 +382,8 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
 }
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
-// kTcVariant the tensor-core kernel (FP32).
+// kTcVariant the tensor-core kernel, kStage3Variant + k constant-operator
+// variant k (both FP32).
 bool set_variant(dg_ctx* c, int v) {
   if (v < 0) {
     c->variant = -1;
@@ -382,6 +391,19 @@ bool set_variant(dg_ctx* c, int v) {
   }
   dgk::Stage2Info si = stage2_info(c, v);
   if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return false;
+  if (v >= dgk::kStage3Variant) {
+    // the constant-operator kernels read Dt [r][i][j] and LIFT [k][i] from
+    // constant memory (uploaded once per device and element type)
+    const int np = c->re.np, D = c->re.dim, nk = c->re.nf * c->re.nfp;
+    std::vector<float> dt((size_t)D * np * np), lift((size_t)nk * np);
+    for (size_t i = 0; i < dt.size(); ++i) dt[i] = (float)c->re.Dt[i];
+    for (int k = 0; k < nk; ++k)
+      for (int i = 0; i < np; ++i) lift[(size_t)k * np + i] = (float)c->re.LIFT[(size_t)i * nk + k];
+    if (dgk::stage3_upload_ops(c->dim, c->order, dt.data(), lift.data()) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
   c->variant = v;
   c->s2 = si;
   c->grid2 = (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms);
@@ -406,6 +428,11 @@ int select_variant(dg_ctx* c, int want) {
   {
     dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
     if (si.nc > 0 && si.blocks_per_sm > 0) cands.push_back(dgk::kTcVariant);
+  }
+  for (int k = 0; k < 8; ++k) {
+    dgk::Stage2Info si = stage2_info(c, dgk::kStage3Variant + k);
+    if (si.nc == 0) break;
+    if (si.blocks_per_sm > 0) cands.push_back(dgk::kStage3Variant + k);
   }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -636,6 +663,11 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
     if (si.nc > 0)
       c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
+  }
+  for (int k = 0; k < 8; ++k) {
+    dgk::Stage2Info si = stage2_info(c, dgk::kStage3Variant + k);
+    if (si.nc == 0) break;
+    c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
   }
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->partials, c->max_grid * 5 * sizeof(double));
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_err, sizeof(int));

@@ -111,6 +111,14 @@ Stage2Info stage2_info_f64_3d(int order, int variant);
 constexpr int kTcVariant = 16;
 cudaError_t launch_stage_tc(int dim, int order, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
 Stage2Info stage_tc_info(int dim, int order);
+// Constant-operator stage kernel (stage3.cuh, FP32 state only): variant ids
+// kStage3Variant + k of the context's kernel selection; the operators are
+// uploaded to constant memory once per device and element type.
+constexpr int kStage3Variant = 32;
+cudaError_t stage3_upload_ops(int dim, int order, const float* Dt, const float* LIFT);
+cudaError_t launch_stage3(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,
+                          cudaStream_t s);
+Stage2Info stage3_info(int dim, int order, int variant);
 // element padding: every tile size divides this
 constexpr int kElemAlign = 128;
 

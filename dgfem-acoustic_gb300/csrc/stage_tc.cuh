@@ -600,14 +600,29 @@ struct StageTc {
       cudaGetLastError();
       return 0;
     }
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, C::NT, C::bytes) != cudaSuccess) {
+    // The runtime's occupancy query answers 1 block per SM for kernels that
+    // use tensor memory; the block count is taken from the SM's limits
+    // instead: shared memory, threads, registers, and the 512 tensor-memory
+    // columns that the resident blocks share. Blocks never wait on one
+    // another, so a grid larger than what is resident is only slower.
+    int dev = 0, smem_sm = 0, smem_res = 0, thr_sm = 0, regs_sm = 0;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_res, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, kfn) != cudaSuccess) {
       cudaGetLastError();
       return 0;
     }
-    // resident blocks of one SM share its 512 tensor-memory columns
+    int nb = smem_sm / ((int)C::bytes + smem_res);
+    nb = nb < thr_sm / C::NT ? nb : thr_sm / C::NT;
+    const int regs_block = ((fa.numRegs + 7) / 8 * 8) * C::NT;
+    if (regs_block > 0) nb = nb < regs_sm / regs_block ? nb : regs_sm / regs_block;
     const int by_tmem = 512 / C::TCOLS;
-    return nb < by_tmem ? nb : by_tmem;
+    nb = nb < by_tmem ? nb : by_tmem;
+    return nb > 0 ? nb : 0;
   }
   static cudaError_t launch(const StageArgs<float>& a, int grid, int* err, cudaStream_t s) {
     auto kfn = stage_tc_kernel<D, P>;

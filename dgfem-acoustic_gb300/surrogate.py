@@ -19,12 +19,15 @@ STEPS RK4 steps (the settled part: the first samples hold the wave-front
 arrival), Hann-tapered and power-normalised, go through the project's
 restatement of the reference's PSD_spec (host.spectra: mean removed,
 one-sided periodogram, src/fft.cpp:183-227); the linear power is averaged
-over 128 bins of width F_MAX/128 (interpolated at the bin centre where a bin
-holds no FFT line) and expressed in dB re (20 uPa)^2, floored DYN_RANGE_DB
-below each observer's peak bin. The taper replaces the rectangular window's
-leakage pattern, which oscillates with f times the window length (and so
-with f, p and M) faster than the parameter sampling resolves, by a compact
-main lobe. Instances use one fixed jittered GRID x GRID mesh per order, so the
+over 128 bins of the source-frequency axis nu = f'/f in [0, NU_MAX)
+(interpolated at the bin centre where a bin holds no FFT line; bin_frequencies
+maps them back to Hz) and expressed in dB re (20 uPa)^2, floored
+DYN_RANGE_DB below each observer's peak bin. The taper replaces the
+rectangular window's leakage pattern, which oscillates with f times the
+window length (and so with f, p and M) faster than the parameter sampling
+resolves, by a compact main lobe; the relative axis keeps the tone at nu = 1
+for every query, so that the network learns its level and lobe shape rather
+than a peak sliding across fixed bins. Instances use one fixed jittered GRID x GRID mesh per order, so the
 spectrum is a function of the six parameters alone.
 """
 import importlib
@@ -35,8 +38,8 @@ import numpy as np
 
 WIDTHS = [6, 256, 256, 256, 256, 512]
 N_OBS, N_BINS = 4, 128
-F_MAX = 2000.0
-DYN_RANGE_DB = 80.0
+NU_MAX = 4.0  # bins span [0, NU_MAX) source-frequency multiples
+DYN_RANGE_DB = 60.0
 STEPS = 3000
 GRID = 25
 MESH_SEEDS = {2: 502, 3: 503, 4: 504}
@@ -72,9 +75,15 @@ def features(params):
     return x
 
 
-def log_psd_bins(trace, dt):
-    """128-bin log-PSD (dB re (20 uPa)^2) of one pressure trace: the last
-    power-of-two samples (the settled part of the run), Hann-tapered and
+def bin_frequencies(f):
+    """Centre frequencies (Hz) of the 128 bins for source frequency f."""
+    return (np.arange(N_BINS) + 0.5) * (NU_MAX / N_BINS) * f
+
+
+def log_psd_bins(trace, dt, f):
+    """128-bin log-PSD (dB re (20 uPa)^2) of one pressure trace on the
+    source-frequency axis nu = f'/f in [0, NU_MAX): the last power-of-two
+    samples (the settled part of the run), Hann-tapered and
     power-normalised, through the PSD_spec restatement."""
     tr = np.asarray(trace, dtype=np.float64)
     n = 1
@@ -84,14 +93,14 @@ def log_psd_bins(trace, dt):
     w = 0.5 * (1.0 - np.cos(2 * np.pi * np.arange(n) / (n - 1)))
     seg = (seg - seg.mean()) * w / math.sqrt(np.mean(w * w))
     _, psd = _pkg().host.spectra(seg.astype(np.float32), dt)
-    f, P = psd[:, 0], psd[:, 1]
-    edges = np.arange(N_BINS + 1) * (F_MAX / N_BINS)
-    idx = np.searchsorted(edges, f, side="right") - 1
+    fl, P = psd[:, 0], psd[:, 1]
+    edges = np.arange(N_BINS + 1) * (NU_MAX / N_BINS) * f
+    idx = np.searchsorted(edges, fl, side="right") - 1
     ok = (idx >= 0) & (idx < N_BINS)
     s = np.bincount(idx[ok], weights=P[ok], minlength=N_BINS)
     c = np.bincount(idx[ok], minlength=N_BINS)
     centres = 0.5 * (edges[:-1] + edges[1:])
-    out = np.where(c > 0, s / np.maximum(c, 1), np.interp(centres, f, P))
+    out = np.where(c > 0, s / np.maximum(c, 1), np.interp(centres, fl, P))
     peak = out.max()
     out = np.maximum(out, peak * 10 ** (-DYN_RANGE_DB / 10) if peak > 0 else 1e-30)
     return 10 * np.log10(out / (2e-5) ** 2)
@@ -134,7 +143,7 @@ def dg_spectra(params, chunk=2000, steps=STEPS, grid=GRID, precision=None, progr
         B.close()
         for k, i in enumerate(insts):
             for o in range(N_OBS):
-                out[c0 + k, o] = log_psd_bins(traces[k][:, o], i["dt"])
+                out[c0 + k, o] = log_psd_bins(traces[k][:, o], i["dt"], i["src"][5])
         if progress:
             progress(c0 + len(rows), P.shape[0])
     return out, dg_s

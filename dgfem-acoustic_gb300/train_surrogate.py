@@ -32,7 +32,7 @@ def main():
     ap.add_argument("--n-train", type=int, default=20000)
     ap.add_argument("--n-test", type=int, default=2000)
     ap.add_argument("--n-calib", type=int, default=2000)
-    ap.add_argument("--train-steps", type=int, default=30000)
+    ap.add_argument("--train-steps", type=int, default=60000)
     ap.add_argument("--dg-steps", type=int, default=3000)
     ap.add_argument("--grid", type=int, default=25)
     ap.add_argument("--bound-db", type=float, default=1.0)

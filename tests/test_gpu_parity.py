@@ -29,14 +29,12 @@ def _mesh(pkg, dim, p, reflect=True):
 
 
 def kernel_variants(pkg, S):
-    """-1 (baseline kernel) and every pipelined variant available for S."""
+    """-1 (baseline kernel) and every other stage-kernel variant available
+    for S: pipelined (0..), tensor-core (16), constant-operator (32..)."""
     out = [-1]
-    for v in range(8):
-        try:
-            S.tune(v)
-        except pkg.gpu.SolverError:
-            break
-        out.append(v)
+    for v in list(range(8)) + [16] + list(range(32, 40)):
+        if S.kernel_info(v)[0] > 0:
+            out.append(v)
     return out
 
 
@@ -95,8 +93,9 @@ def _sources_observers(mesh, srcs, obs):
     return sdofs, odofs, ows
 
 
-@pytest.mark.parametrize("variant", [-1, 0, 1])
-@pytest.mark.parametrize("dim,p,prec", [(2, 3, "fp64"), (3, 2, "fp64"), (3, 3, "fp64"), (2, 3, "fp32"), (3, 3, "fp32")])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 32, 33])
+@pytest.mark.parametrize("dim,p,prec", [(2, 3, "fp64"), (3, 2, "fp64"), (3, 3, "fp64"), (2, 3, "fp32"), (3, 3, "fp32"),
+                                        (2, 4, "fp32"), (2, 2, "fp32")])
 def test_run_parity(pkg, oracle, dim, p, prec, variant):
     mesh = _mesh(pkg, dim, p)
     ph = _phys(dim)
@@ -109,6 +108,8 @@ def test_run_parity(pkg, oracle, dim, p, prec, variant):
     ref = P.run()
     assert ref["steps"] == nsteps
     S = pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
+    if S.kernel_info(variant)[0] == 0:
+        pytest.skip("variant %d does not exist for this element type and precision" % variant)
     S.tune(variant)
     S.set_state(P.initial_state())
     sdofs, odofs, ows = _sources_observers(mesh, [src], obs)
@@ -135,4 +136,8 @@ def test_run_parity(pkg, oracle, dim, p, prec, variant):
     assert rel_l2(u[:nv], ref["state"][:nv]) <= tol
     assert rel_l2(res[:, :4], ref["residuals"][:, :4]) <= (1e-10 if prec == "fp64" else 1e-3)
     ob_ref = ref["obs"][:, :, [1, 2, 3, 4]]  # p, vx, vy, vz
-    assert rel_l2(tr, ob_ref) <= tol * 10
+    # an observer with no DG node in its radius reports NaN in both (the
+    # reference's rule)
+    ok = np.isfinite(ob_ref)
+    assert np.array_equal(np.isfinite(tr), ok)
+    assert rel_l2(tr[ok], ob_ref[ok]) <= tol * 10
