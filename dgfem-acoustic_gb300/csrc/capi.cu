@@ -943,7 +943,8 @@ int dg_kernel_info(dg_ctx* c, int variant, int* out) {
     return DG_OK;
   }
   dgk::Stage2Info si = stage2_info(c, variant);
-  if (si.nc == 0) return DG_OK;
+  // available exactly when dg_tune accepts it
+  if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return DG_OK;
   out[0] = si.et, out[1] = si.nt, out[2] = si.smem_bytes, out[3] = si.blocks_per_sm;
   out[4] = (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms);
   return DG_OK;
