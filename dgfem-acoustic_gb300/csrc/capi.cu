@@ -411,8 +411,9 @@ bool set_variant(dg_ctx* c, int v) {
   return true;
 }
 
-// Autotuner: times one RK stage (stage 2: reads y, u, acc; writes acc, y) of
-// every kernel variant on this mesh and keeps the fastest. want >= -1 forces
+// Autotuner: times RK stages 1-3 (stage input, u and accumulator reads;
+// accumulator and next-stage writes) of every kernel variant on this mesh
+// and keeps the fastest. want >= -1 forces
 // a variant instead.
 int select_variant(dg_ctx* c, int want) {
   if (want >= -1) {
@@ -441,10 +442,13 @@ int select_variant(dg_ctx* c, int want) {
   int best_v = -1;
   for (int v : cands) {
     if (!set_variant(c, v)) continue;
+    // stages 1-3 of an RK step (their operand mixes differ; stage 4 would
+    // write the state), once to warm up, then three times timed
     cudaError_t err = cudaSuccess;
-    for (int r = 0; r < 2 && err == cudaSuccess; ++r) err = launch_stage(c, 2, c->y0, c->y1, nullptr, 1e-30);
+    for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
     cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < 4 && err == cudaSuccess; ++r) err = launch_stage(c, 2, c->y0, c->y1, nullptr, 1e-30);
+    for (int r = 0; r < 3; ++r)
+      for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
     cudaEventRecord(e1, c->stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
     if (err != cudaSuccess) {
@@ -458,8 +462,7 @@ int select_variant(dg_ctx* c, int want) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  int zero = 0;
-  cudaMemcpy(c->d_err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   // the timing runs wrote the accumulator and stage buffers only; clear them
   const size_t nb = (size_t)c->nv * c->Epad * c->np * c->tsize;
   cudaMemsetAsync(c->acc, 0, nb, c->stream);
@@ -631,27 +634,27 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
   std::vector<short> fm(c->re.fmask.begin(), c->re.fmask.end()), nb(c->re.nbrnode.begin(), c->re.nbrnode.end());
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->fmask, fm.size() * sizeof(short));
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->nbrnode, nb.size() * sizeof(short));
-  if (e == cudaSuccess) e = cudaMemcpy(c->fmask, fm.data(), fm.size() * sizeof(short), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(c->nbrnode, nb.data(), nb.size() * sizeof(short), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->fmask, fm.data(), fm.size() * sizeof(short), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->nbrnode, nb.data(), nb.size() * sizeof(short), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
     if (c->prec == DG_FP32) {
       std::vector<float> Dt, L;
       to_dev_ops(c->re, Dt, L);
       e = dgc::dev_alloc(c, &c->Dt, Dt.size() * 4);
       if (e == cudaSuccess) e = dgc::dev_alloc(c, &c->LIFT, L.size() * 4);
-      if (e == cudaSuccess) e = cudaMemcpy(c->Dt, Dt.data(), Dt.size() * 4, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMemcpy(c->LIFT, L.data(), L.size() * 4, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(c->Dt, Dt.data(), Dt.size() * 4, cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(c->LIFT, L.data(), L.size() * 4, cudaMemcpyHostToDevice, c->stream);
     } else {
       std::vector<double> Dt, L;
       to_dev_ops(c->re, Dt, L);
       e = dgc::dev_alloc(c, &c->Dt, Dt.size() * 8);
       if (e == cudaSuccess) e = dgc::dev_alloc(c, &c->LIFT, L.size() * 8);
-      if (e == cudaSuccess) e = cudaMemcpy(c->Dt, Dt.data(), Dt.size() * 8, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMemcpy(c->LIFT, L.data(), L.size() * 8, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(c->Dt, Dt.data(), Dt.size() * 8, cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(c->LIFT, L.data(), L.size() * 8, cudaMemcpyHostToDevice, c->stream);
     }
   }
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_perm, c->np * sizeof(int));
-  if (e == cudaSuccess) e = cudaMemcpy(c->d_perm, c->perm_c2i.data(), c->np * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_perm, c->perm_c2i.data(), c->np * sizeof(int), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = dgc::dev_alloc(c, (void**)&c->d_ref, 4 * c->E * c->np * sizeof(double));
   c->max_grid = std::max(c->grid, 2 * c->num_sms);
   for (int v = 0; v < 8; ++v) {
@@ -799,9 +802,12 @@ int dg_set_sources(dg_ctx* c, int n_src, const int64_t* offsets, const int64_t* 
   CK(c, cudaMalloc(&c->d_src_dof, hd.size() * sizeof(int64_t)));
   CK(c, cudaMalloc(&c->d_src_off, ho.size() * sizeof(int)));
   CK(c, cudaMalloc(&c->d_src_ids, hi.size() * sizeof(int)));
-  CK(c, cudaMemcpy(c->d_src_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-  CK(c, cudaMemcpy(c->d_src_off, ho.data(), ho.size() * sizeof(int), cudaMemcpyHostToDevice));
-  CK(c, cudaMemcpy(c->d_src_ids, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpyAsync(c->d_src_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpyAsync(c->d_src_off, ho.data(), ho.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpyAsync(c->d_src_ids, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   return DG_OK;
 }
 
@@ -812,7 +818,8 @@ int dg_set_source_values(dg_ctx* c, int64_t n_steps, const double* values) {
   if (c->graph) cudaGraphExecDestroy(c->graph), c->graph = nullptr;
   if (n_steps == 0 || c->n_src == 0) return DG_OK;
   CK(c, cudaMalloc(&c->d_srcval, n_steps * c->n_src * sizeof(double)));
-  CK(c, cudaMemcpy(c->d_srcval, values, n_steps * c->n_src * sizeof(double), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpyAsync(c->d_srcval, values, n_steps * c->n_src * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   c->srcval_steps = n_steps;
   return DG_OK;
 }
@@ -840,9 +847,14 @@ int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t
   CK(c, cudaMalloc(&c->d_obs_dof, hd.size() * sizeof(int64_t)));
   CK(c, cudaMalloc(&c->d_obs_off, (n_obs + 1) * sizeof(int64_t)));
   CK(c, cudaMalloc(&c->d_obs_w, std::max<int64_t>(total, 1) * sizeof(double)));
-  CK(c, cudaMemcpy(c->d_obs_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-  CK(c, cudaMemcpy(c->d_obs_off, offsets, (n_obs + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-  if (total > 0) CK(c, cudaMemcpy(c->d_obs_w, weights, total * sizeof(double), cudaMemcpyHostToDevice));
+  CK(c, cudaMemcpyAsync(c->d_obs_dof, hd.data(), hd.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  CK(c, cudaMemcpyAsync(c->d_obs_off, offsets, (n_obs + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (total > 0) {
+    CK(c, cudaMemcpyAsync(c->d_obs_w, weights, total * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
   return DG_OK;
 }
 
@@ -919,9 +931,13 @@ int dg_face_info(dg_ctx* c, int64_t* nbr, int* penalty, int* bc) {
   if (!c) return DG_ERR_ARG;
   const int reci = c->sh.reci, nf = c->nf;
   std::vector<int> gi(c->E * reci);
-  CK(c, cudaMemcpy(gi.data(), c->geoI, gi.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpyAsync(gi.data(), c->geoI, gi.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   std::vector<int> bcodes(std::max<int64_t>(c->n_bfaces, 1));
-  if (c->n_bfaces > 0) CK(c, cudaMemcpy(bcodes.data(), c->d_bcode, c->n_bfaces * sizeof(int), cudaMemcpyDeviceToHost));
+  if (c->n_bfaces > 0) {
+    CK(c, cudaMemcpyAsync(bcodes.data(), c->d_bcode, c->n_bfaces * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
   for (int64_t e = 0; e < c->E; ++e)
     for (int lf = 0; lf < nf; ++lf) {
       int nb = gi[e * reci + lf], code = gi[e * reci + nf + lf];

@@ -332,8 +332,11 @@ int dg_mlp_create(int n_layers, const int* widths, int device, dg_mlp** out) {
   if (e == cudaSuccess) e = cudaMalloc(&m->wh, m->n_wts * sizeof(__nv_bfloat16));
   if (e == cudaSuccess) e = cudaMalloc(&m->part, 64 * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&m->loss, sizeof(double));
+  // on the network's own (non-blocking) stream: a legacy-stream memset would
+  // not be ordered with the uploads that follow
   for (float* q : {m->p, m->g, m->m1, m->m2})
-    if (e == cudaSuccess) e = cudaMemset(q, 0, m->n_params * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemsetAsync(q, 0, m->n_params * sizeof(float), m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
   if (e != cudaSuccess) {
     std::string msg = std::string("dg_mlp_create: CUDA: ") + cudaGetErrorString(e);
     dg_mlp_destroy(m);
