@@ -251,6 +251,27 @@ def run_ensemble(args):
         ms = B.bench(args.steps)
     batched = dofs / (ms * 1e-3)
     B.close()
+    peak, peak_kind = measured_peak_gbs()
+    rec_bytes = geometry_record_words(2, 4) * 4 + 8 * 4
+
+    def alg_bytes(subset):
+        # 18 state words per DOF and 4 geometry records per element per step
+        d = sum(i["mesh"]["elem_nodes"].size * 3 for i in subset)
+        e = sum(i["mesh"]["elem_nodes"].shape[0] for i in subset)
+        return d, 18 * d * 4 + 4 * e * rec_bytes
+
+    # the same instances, one batch per element order, timed alone
+    per_order = {}
+    for p in (2, 3, 4):
+        sub = [i for i in insts if i["p"] == p]
+        Bp = make(pkg.gpu.DG_FP32, sub)
+        Bp.run(args.warmup)
+        msp = Bp.bench(args.steps)
+        Bp.close()
+        d, bts = alg_bytes(sub)
+        per_order[str(p)] = {"instances": len(sub), "dofs": d, "ms_per_step": msp, "dof_updates_per_s": d / (msp * 1e-3),
+                             "hbm_frac": bts / (msp * 1e-3) / 1e9 / peak}
+    _, all_bytes = alg_bytes(insts)
     # plain path: every 32nd instance on its own, same steps
     sample = insts[::32]
     tot_dof, tot_ms = 0, 0.0
@@ -292,6 +313,10 @@ def run_ensemble(args):
             "plain_single_instance": {"value": plain, "unit": UNIT, "sample": "%d instances run one by one"
                                       % len(sample)},
             "batched_over_plain": batched / plain,
+            "roofline": {"bound": "hbm", "achieved": all_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": all_bytes / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_step": int(all_bytes), "time": "whole step (graph)"},
+            "per_order": per_order,
             "fp32_vs_fp64_rel_l2_max": max(errs), "error_steps": nerr, "error_instances": len(sub),
             "clocks": clk.summary()}
 

@@ -438,6 +438,14 @@ int select_variant(dg_ctx* c, int want) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // the caches are flushed before each timed repetition (a write larger than
+  // L2), as a stage of a real step finds them after the other stages' traffic
+  const int64_t flush_words = (int64_t)64 << 20;  // 256 MiB
+  unsigned* flush = nullptr;
+  if (cudaMalloc(&flush, flush_words * sizeof(unsigned)) != cudaSuccess) {
+    cudaGetLastError();
+    flush = nullptr;
+  }
   float best = 1e30f;
   int best_v = -1;
   for (int v : cands) {
@@ -446,20 +454,26 @@ int select_variant(dg_ctx* c, int want) {
     // write the state), once to warm up, then three times timed
     cudaError_t err = cudaSuccess;
     for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
-    cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < 3; ++r)
+    float tot = 0.f;
+    for (int r = 0; r < 3 && err == cudaSuccess; ++r) {
+      if (flush) k_flush<<<2 * c->num_sms, 512, 0, c->stream>>>(flush, flush_words, (unsigned)r);
+      cudaEventRecord(e0, c->stream);
       for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
-    cudaEventRecord(e1, c->stream);
-    if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+      cudaEventRecord(e1, c->stream);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+      float ms = 0.f;
+      if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+      tot += ms;
+    }
     if (err != cudaSuccess) {
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
+      if (flush) cudaFree(flush);
       return fail(c, DG_ERR_CUDA, std::string("CUDA (autotune): ") + cudaGetErrorString(err));
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) best = ms, best_v = v;
+    if (tot < best) best = tot, best_v = v;
   }
+  if (flush) cudaFree(flush);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);

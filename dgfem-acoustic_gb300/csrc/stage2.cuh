@@ -135,18 +135,20 @@ struct RoundUp {
 // sN [NV][ET][NKP].
 
 // Issues cp.async gathers of the neighbour traces of every interior face
-// node of the tile into sN (the caller commits and waits).
+// node of the tile whose neighbour lies outside the tile (elements e0 ..
+// e0+ET-1) into sN (the caller commits and waits); traces of neighbours
+// inside the tile are read from the tile itself by face_fluxes.
 template <class C, typename T>
 __device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_t stride, const int* sGI,
-                                              const short* sNb, T* sN, int tid) {
+                                              const short* sNb, T* sN, int tid, int64_t e0) {
   constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
   constexpr int ET = C::ET, NT = C::NT, RECI = C::RECI;
   for (int q8 = tid; q8 < ET * NK; q8 += NT) {
     const int el = q8 / NK, k = q8 - el * NK;
     const int f = k / NFP, m = k - f * NFP;
     const int code = sGI[el * RECI + NF + f];
-    if (!(code & kCodeBoundary)) {
-      const int nbr = sGI[el * RECI + f];
+    const int nbr = sGI[el * RECI + f];
+    if (!(code & kCodeBoundary) && (uint64_t)((int64_t)nbr - e0) >= (uint64_t)ET) {
       const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
       const T* src = y_in + (int64_t)nbr * NP + nn;
 #pragma unroll
@@ -164,11 +166,14 @@ __device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_
 // Face numerical fluxes of every face node of the tile, scaled by the face
 // scale sJ, written in place of the gathered traces in sN: the interior
 // Lax-Friedrichs flux (src/Mesh.cpp:761-813) or the boundary matrix
-// (absorbing RKR / reflecting, src/Mesh.cpp:882-972).
+// (absorbing RKR / reflecting, src/Mesh.cpp:882-972). The neighbour trace
+// comes from the tile when the neighbour is one of its elements, else from
+// the gathered copy.
 template <class C, typename T>
 __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T* sY, const T* sGF, const int* sGI,
-                                            const short* sFm, T* sN, int tid, T rhoc2, T inv_rho0, T half_c0) {
-  constexpr int D = C::D, NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NK = C::NK;
+                                            const short* sFm, const short* sNb, T* sN, int tid, T rhoc2, T inv_rho0,
+                                            T half_c0, int64_t e0) {
+  constexpr int D = C::D, NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NK = C::NK, NPERM = C::NPERM;
   constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
   for (int q8 = tid; q8 < ET * NK; q8 += NT) {
     const int el = q8 / NK, k = q8 - el * NK;
@@ -197,8 +202,16 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
       }
     } else {
       T up[NV];
+      const int64_t rel = (int64_t)nbr - e0;
+      if ((uint64_t)rel < (uint64_t)ET) {
+        const int m = k - f * NFP;
+        const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
+        for (int q = 0; q < NV; ++q) up[q] = sY[(q * ET + (int)rel) * NP + nn];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
+      }
       const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
       const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
       T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
@@ -337,7 +350,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       if (nepi > 0) issue_epi(tile);
     }
     // ---- neighbour traces: asynchronous gathers into sN ----
-    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid);
+    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
     cp_async_commit();
 
     // ---- volume term for this thread's nodes ----
@@ -402,7 +415,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     __syncthreads();
 
     // ---- face numerical fluxes (in place of the gathered traces) ----
-    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sN, tid, rhoc2, inv_rho0, half_c0);
+    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
     __syncthreads();
 
     // ---- lifting ----

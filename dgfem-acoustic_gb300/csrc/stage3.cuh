@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
       prefetch_l2(src + q * stride + e0 * NP, C::YSEG);
     }
     // ---- neighbour traces (asynchronous) ----
-    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid);
+    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
     cp_async_commit();
     // ---- element-minor copy of the stage input ----
     for (int w = tid; w < NV * ET * NP; w += NT) {
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
     cp_async_wait_all();
     __syncthreads();
     // ---- face numerical fluxes (in place of the gathered traces) ----
-    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sN, tid, rhoc2, inv_rho0, half_c0);
+    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
     __syncthreads();
 
     // ---- volume and lift for this warp's node chunk ----

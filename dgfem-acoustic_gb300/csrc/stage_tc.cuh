@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
       if (nepi > 0) issue_epi(tile), arm(2, it);
     }
     // ---- neighbour traces (asynchronous) ----
-    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid);
+    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
     cp_async_commit();
     // ---- per-element values of the row phase, element-minor ----
     for (int w = tid; w < ET * GT; w += NT) {
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
     __syncthreads();
 
     // ---- face numerical fluxes (in place of the gathered traces) ----
-    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sN, tid, rhoc2, inv_rho0, half_c0);
+    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
     __syncthreads();
 
     // ---- face rows: A_face[(q,e)][k] -> tensor memory ----

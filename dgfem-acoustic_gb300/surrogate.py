@@ -39,7 +39,7 @@ import numpy as np
 WIDTHS = [6, 256, 256, 256, 256, 512]
 N_OBS, N_BINS = 4, 128
 NU_MAX = 4.0  # bins span [0, NU_MAX) source-frequency multiples
-DYN_RANGE_DB = 60.0
+DYN_RANGE_DB = 30.0
 STEPS = 3000
 GRID = 25
 MESH_SEEDS = {2: 502, 3: 503, 4: 504}
