@@ -365,7 +365,8 @@ def run_ensemble_profile(args):
     """Warm-up plus a few steps of the 256-instance ensemble (FP32 batch),
     nothing else (the command line of the ensemble ncu summaries)."""
     pkg = _pkg()
-    insts = pkg.ensemble.draw_instances(256, seed=4)
+    keep = {int(o) for o in args.orders.split(",")}
+    insts = [i for i in pkg.ensemble.draw_instances(256, seed=4) if i["p"] in keep]
     B = pkg.ensemble.make_batch(insts, pkg.gpu.DG_FP32, args.warmup + args.steps + 2)
     B.run(args.warmup)
     obs = B.run(args.steps)
@@ -444,6 +445,8 @@ def main():
     ap.add_argument("--variant", type=int, default=-2,
                     help="stage kernel variant (-2: autotuned at setup, -1: baseline kernel, k: pipelined variant k)")
     ap.add_argument("--workload", default="cube", choices=["cube", "ensemble", "surrogate"])
+    ap.add_argument("--orders", default="2,3,4",
+                    help="ensemble workload: element orders of the instances to keep (profiling subsets)")
     ap.add_argument("--profile", action="store_true",
                     help="only build the workload and run warmup + steps time steps (for ncu captures)")
     args = ap.parse_args()
