@@ -157,16 +157,18 @@ __global__ void k_gather_rows(const float* __restrict__ src, const int* __restri
   dst[i] = src[(int64_t)idx[r] * w + c];
 }
 
-// Adam on the FP32 master parameters; weights are re-rounded to BF16
+// Adam on the FP32 master parameters with decoupled weight decay wd (AdamW);
+// weights are re-rounded to BF16 afterwards
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
-                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       float wd) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
   const float a = b1 * m1[i] + (1.f - b1) * gi;
   const float v = b2 * m2[i] + (1.f - b2) * gi * gi;
   m1[i] = a, m2[i] = v;
-  p[i] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
+  p[i] -= lr * ((a / c1) / (sqrtf(v / c2) + eps) + wd * p[i]);
 }
 
 __global__ void k_to_bf16(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, int64_t n) {
@@ -456,8 +458,9 @@ int dg_mlp_set_data(dg_mlp* m, const float* x, const float* t, int64_t n) {
   return DG_OK;
 }
 
-int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, uint64_t seed, double* losses) {
-  if (!m || n_steps < 0 || batch < 1 || !(lr > 0) || !(lr_final > 0))
+int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, double weight_decay, uint64_t seed,
+                 double* losses) {
+  if (!m || n_steps < 0 || batch < 1 || !(lr > 0) || !(lr_final > 0) || !(weight_decay >= 0))
     return fail(m, DG_ERR_ARG, "dg_mlp_train: invalid argument");
   if (m->n_data < batch) return fail(m, DG_ERR_ARG, "dg_mlp_train: fewer training rows than one batch");
   cudaSetDevice(m->device);
@@ -502,7 +505,7 @@ int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_fin
     m->step += 1;
     const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
     k_adam<<<nblk(m->n_params, 256), 256, 0, m->stream>>>(m->p, m->g, m->m1, m->m2, m->n_params, (float)lrs, b1, b2,
-                                                          eps, c1, c2);
+                                                          eps, c1, c2, (float)weight_decay);
     rc = refresh_bf16(m);
     if (e == cudaSuccess) e = cudaGetLastError();
   }

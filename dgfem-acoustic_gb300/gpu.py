@@ -384,7 +384,7 @@ def _mlp_lib():
     L.dg_mlp_forward_device.argtypes = [C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p]
     L.dg_mlp_gradient.argtypes = [C.c_void_p, P(F), P(F), I64, P(F), P(D)]
     L.dg_mlp_set_data.argtypes = [C.c_void_p, P(F), P(F), I64]
-    L.dg_mlp_train.argtypes = [C.c_void_p, I64, C.c_int, D, D, C.c_uint64, P(D)]
+    L.dg_mlp_train.argtypes = [C.c_void_p, I64, C.c_int, D, D, D, C.c_uint64, P(D)]
     L._mlp = True
     return L
 
@@ -459,7 +459,8 @@ class Network:
         self._t = np.ascontiguousarray(t, dtype=np.float32).reshape(self._x.shape[0], self.widths[-1])
         self._ck(_mlp_lib().dg_mlp_set_data(self.h, _fp(self._x), _fp(self._t), self._x.shape[0]), "dg_mlp_set_data")
 
-    def train(self, n_steps, batch, lr, lr_final, seed=0):
+    def train(self, n_steps, batch, lr, lr_final, seed=0, weight_decay=0.0):
         losses = np.zeros(max(n_steps, 1))
-        self._ck(_mlp_lib().dg_mlp_train(self.h, n_steps, batch, lr, lr_final, seed, _dp(losses)), "dg_mlp_train")
+        self._ck(_mlp_lib().dg_mlp_train(self.h, n_steps, batch, lr, lr_final, weight_decay, seed, _dp(losses)),
+                 "dg_mlp_train")
         return losses[:n_steps]

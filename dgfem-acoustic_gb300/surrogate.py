@@ -156,8 +156,8 @@ def rms_db(a, b):
 
 
 class Surrogate:
-    """Two independently trained networks, target normalisation and the
-    calibrated error estimate."""
+    """Independently trained networks (two by default), target normalisation
+    and the calibrated error estimate (the members' spread)."""
 
     def __init__(self, params_list, mu, sigma, scale=1.0, grid=GRID, steps=STEPS, device=0):
         self.mu = np.asarray(mu, dtype=np.float32)
@@ -172,7 +172,7 @@ class Surrogate:
 
     @classmethod
     def fit(cls, params, targets, n_models=2, steps=20000, batch=256, lr=2e-3, lr_final=2e-5, seed=0, grid=GRID,
-            dg_steps=STEPS, device=0):
+            dg_steps=STEPS, weight_decay=0.0, device=0):
         x = features(params)
         y = np.asarray(targets, dtype=np.float64).reshape(len(x), -1)
         mu = y.mean(axis=0)
@@ -184,7 +184,8 @@ class Surrogate:
             net = _pkg().gpu.Network(WIDTHS, device=device)
             net.set_params(_init(WIDTHS, int(rng.integers(1 << 30))))
             net.set_data(x, t)
-            losses.append(net.train(steps, batch, lr, lr_final, seed=int(rng.integers(1 << 62))))
+            losses.append(net.train(steps, batch, lr, lr_final, seed=int(rng.integers(1 << 62)),
+                                    weight_decay=weight_decay))
             plist.append(net.get_params())
             net.close()
         s = cls(plist, mu, sigma, grid=grid, steps=dg_steps, device=device)
@@ -198,7 +199,8 @@ class Surrogate:
         ys = [net.forward(x).astype(np.float64) * self.sigma + self.mu for net in self.nets]
         mean = np.mean(ys, axis=0)
         if len(ys) > 1:
-            est = self.scale * rms_db(ys[0], ys[1])
+            # spread of the members around their mean (RMS over outputs)
+            est = self.scale * np.sqrt(np.mean([rms_db(y, mean) ** 2 for y in ys], axis=0) * len(ys) / (len(ys) - 1))
         else:
             est = np.zeros(len(x))
         return mean.reshape(-1, N_OBS, N_BINS), est

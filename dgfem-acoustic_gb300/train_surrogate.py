@@ -36,13 +36,16 @@ def main():
     ap.add_argument("--dg-steps", type=int, default=3000)
     ap.add_argument("--grid", type=int, default=25)
     ap.add_argument("--bound-db", type=float, default=1.0)
+    ap.add_argument("--models", type=int, default=2)
+    ap.add_argument("--weight-decay", type=float, default=0.0)
     args = ap.parse_args()
     sys.path.insert(0, ROOT)
     pkg = importlib.import_module("dgfem-acoustic_gb300")
     S = pkg.surrogate
     os.makedirs(args.out, exist_ok=True)
     rep = {"n_train": args.n_train, "n_test": args.n_test, "n_calib": args.n_calib, "dg_steps": args.dg_steps,
-           "grid": args.grid, "bound_db": args.bound_db}
+           "grid": args.grid, "bound_db": args.bound_db, "models": args.models, "weight_decay": args.weight_decay,
+           "train_steps": args.train_steps}
 
     P_train = S.draw_params(args.n_train, 5)
     P_test = S.draw_params(args.n_test, 6)
@@ -55,8 +58,8 @@ def main():
 
     nfit = args.n_train - args.n_calib
     t0 = time.perf_counter()
-    sur = S.Surrogate.fit(P_train[:nfit], Y_train[:nfit], steps=args.train_steps, grid=args.grid,
-                          dg_steps=args.dg_steps)
+    sur = S.Surrogate.fit(P_train[:nfit], Y_train[:nfit], n_models=args.models, steps=args.train_steps,
+                          grid=args.grid, dg_steps=args.dg_steps, weight_decay=args.weight_decay)
     rep["train_s"] = time.perf_counter() - t0
     rep["final_train_loss"] = [float(np.mean(l[-200:])) for l in sur.train_losses]
     rep["calibration_scale"] = sur.calibrate(P_train[nfit:], Y_train[nfit:])
@@ -85,6 +88,20 @@ def main():
     rep["surrogate_queries_per_s"] = args.n_test / sur_s
     rep["dg_queries_per_s"] = args.n_test / dg_s_test
     rep["speedup"] = rep["surrogate_queries_per_s"] / rep["dg_queries_per_s"]
+    # the surrogate with its DG fallback at several bounds: the accepted
+    # queries, their true error, and the throughput of the combined answer
+    # (accepted queries from the network, the others re-run through DG)
+    rep["by_bound"] = {}
+    for b in (1.0, 2.0, 3.0, 5.0):
+        acc_b = est <= b
+        frac = float(acc_b.mean())
+        t_per_q = (1 - frac) / rep["dg_queries_per_s"] + 1 / rep["surrogate_queries_per_s"]
+        rep["by_bound"][str(b)] = {
+            "accepted_fraction": frac,
+            "accepted_rms_db_p95": float(np.quantile(err[acc_b], 0.95)) if acc_b.any() else None,
+            "accepted_above_bound_fraction": float(np.mean(err[acc_b] > b)) if acc_b.any() else None,
+            "queries_per_s_with_fallback": 1.0 / t_per_q,
+            "speedup_over_dg": 1.0 / t_per_q / rep["dg_queries_per_s"]}
     with open(os.path.join(args.out, "report.json"), "w") as f:
         json.dump(rep, f, indent=1)
     print(json.dumps(rep))

@@ -234,10 +234,12 @@ int dg_mlp_forward_device(dg_mlp* m, const float* x, int64_t n, float* y, void* 
 int dg_mlp_gradient(dg_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss);
 /* training rows (host arrays, copied to the device once) */
 int dg_mlp_set_data(dg_mlp* m, const float* x, const float* t, int64_t n);
-/* n_steps Adam steps (beta 0.9/0.999, eps 1e-8) on shuffled mini-batches
- * (one permutation per epoch from seed), learning rate decaying from lr to
- * lr_final on a cosine; losses (optional) receives each step's batch loss */
-int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, uint64_t seed, double* losses);
+/* n_steps Adam steps (beta 0.9/0.999, eps 1e-8, decoupled weight decay
+ * weight_decay, 0 for plain Adam) on shuffled mini-batches (one permutation
+ * per epoch from seed), learning rate decaying from lr to lr_final on a
+ * cosine; losses (optional) receives each step's batch loss */
+int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, double weight_decay, uint64_t seed,
+                 double* losses);
 
 #ifdef __cplusplus
 }
