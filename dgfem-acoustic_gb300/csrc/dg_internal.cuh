@@ -53,6 +53,53 @@ struct ShapeT : Shape<D, P> {
   static constexpr int RECF = (Shape<D, P>::RECF_RAW + VEC - 1) / VEC * VEC;
 };
 
+// Residual partial sums of one thread: mean over the state of
+// (snapshot - u)^2 for p, p/c0^2 and the velocity components
+// (src/solver.cpp:518-545). FP64 states follow the reference's formula in
+// FP64. FP32 states square the FP32 differences and sum them in FP32 (GB300's
+// FP64 rate made this diagnostic the most expensive part of the last RK
+// stage); the density sum is p's sum / c0^4, the same quantity in exact
+// arithmetic. The block reduction that follows is in FP64.
+template <typename T>
+struct ResAcc;
+template <>
+struct ResAcc<double> {
+  double r[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  __device__ __forceinline__ void add(int q, double s, double u, double c0sq) {
+    const double dn = s - u;
+    if (q == 0) {
+      r[0] += dn * dn;
+      const double dr = s / c0sq - u / c0sq;
+      r[1] += dr * dr;
+    } else if (q == 1) {
+      r[2] += dn * dn;
+    } else if (q == 2) {
+      r[3] += dn * dn;
+    } else {
+      r[4] += dn * dn;
+    }
+  }
+  __device__ __forceinline__ double get(int c, double) const { return r[c]; }
+};
+template <>
+struct ResAcc<float> {
+  float r[4] = {0.f, 0.f, 0.f, 0.f};  // p, vx, vy, vz
+  __device__ __forceinline__ void add(int q, float s, float u, double) {
+    const float dn = s - u;
+    if (q == 0)
+      r[0] = fmaf(dn, dn, r[0]);
+    else if (q == 1)
+      r[1] = fmaf(dn, dn, r[1]);
+    else if (q == 2)
+      r[2] = fmaf(dn, dn, r[2]);
+    else
+      r[3] = fmaf(dn, dn, r[3]);
+  }
+  __device__ __forceinline__ double get(int c, double c0sq) const {
+    return c == 0 ? (double)r[0] : c == 1 ? (double)r[0] / (c0sq * c0sq) : (double)r[c - 1];
+  }
+};
+
 // Physical constants used by the kernels.
 struct Phys {
   double v0[3];

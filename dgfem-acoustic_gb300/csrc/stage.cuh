@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
   const int64_t stride = a.stride;
-  double red[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  ResAcc<T> racc;
 
   for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
     const int64_t e0 = (int64_t)tile * ET;
@@ -255,14 +255,7 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
           case 4: {
             const T un = a.u[g] + (a.acc[g] + kv) / (T)6;
             a.u[g] = un;
-            const double dn = (double)a.snap[g] - (double)un;
-            if (q == 0) {
-              red[0] += dn * dn;
-              const double dr = (double)a.snap[g] / a.c0sq - (double)un / a.c0sq;
-              red[1] += dr * dr;
-            } else {
-              red[1 + q] += dn * dn;
-            }
+            racc.add(q, a.snap[g], un, a.c0sq);
             break;
           }
           default:
@@ -278,7 +271,7 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
     // block reduction of the residual partial sums (fixed order: deterministic)
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      double v = red[c];
+      double v = racc.get(c, a.c0sq);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
       if ((tid & 31) == 0) sRed[(tid >> 5) * 5 + c] = v;

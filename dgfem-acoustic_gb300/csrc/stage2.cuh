@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
 
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
-  double red[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  ResAcc<T> racc;
   bool ok = true;
   const int e = tid / NSPLIT, s = tid - (tid / NSPLIT) * NSPLIT;
   const int i0 = s * NC;
@@ -483,15 +483,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
             for (int v = 0; v < VW; ++v) {
               const T un = xu[v] + (xa[v] + kv[v]) / (T)6;
               o1[v] = un;
-              const double sn = (double)xs[v];
-              const double dn = sn - (double)un;
-              if (q == 0) {
-                red[0] += dn * dn;
-                const double dr = sn / a.c0sq - (double)un / a.c0sq;
-                red[1] += dr * dr;
-              } else {
-                red[1 + q] += dn * dn;
-              }
+              racc.add(q, xs[v], un, a.c0sq);
             }
             vstore<T, VW>(a.u + g, o1);
             break;
@@ -512,7 +504,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
   if (stage == 4) {
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      double v = red[c];
+      double v = racc.get(c, a.c0sq);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
       if ((tid & 31) == 0) sRed[(tid >> 5) * 5 + c] = v;

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
 
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
-  double red[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  ResAcc<float> racc;
   bool ok = true;
   const int nepi = (stage == 2 || stage == 3) ? 2 : (stage == 4 ? 3 : 0);
 
@@ -314,20 +314,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
                                xu.w + (xa.w + kv.w) / 6.f};
           const float sn[4] = {xs.x, xs.y, xs.z, xs.w};
 #pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            const double dn = (double)sn[v] - (double)un[v];
-            if (q == 0) {
-              red[0] += dn * dn;
-              const double dr = (double)sn[v] / a.c0sq - (double)un[v] / a.c0sq;
-              red[1] += dr * dr;
-            } else if (q == 1) {
-              red[2] += dn * dn;
-            } else if (q == 2) {
-              red[3] += dn * dn;
-            } else {
-              red[4] += dn * dn;
-            }
-          }
+          for (int v = 0; v < 4; ++v) racc.add(q, sn[v], un[v], a.c0sq);
           *reinterpret_cast<float4*>(a.u + gidx) = make_float4(un[0], un[1], un[2], un[3]);
           break;
         }
@@ -350,7 +337,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
   if (stage == 4) {
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      double v = red[c];
+      double v = racc.get(c, a.c0sq);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
       if (lane == 0) sRed[warp * 5 + c] = v;

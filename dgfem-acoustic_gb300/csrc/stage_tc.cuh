@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
 
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
-  double red_a = 0.0, red_b = 0.0;  // this row's residual sums: (snap-u)^2, and for p also in density units
+  float red_a = 0.f;  // this row's residual sum of (snapshot - u)^2 (FP32, see ResAcc)
   bool ok = true;
   // thread 0: barriers whose armed phase was not yet observed complete (bit i)
   // and that phase's parity (bit 4+i); drained before the block exits
@@ -510,12 +510,8 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
             for (int u = 0; u < 4; ++u) {
               o0[u] = x0[u] + (x1[u] + kv[u]) / (T)6;
               if (i0 + u < NP) {
-                const double sn = (double)gs[i0 + u], dn = sn - (double)o0[u];
-                red_a += dn * dn;
-                if (q == 0) {
-                  const double dr = sn / a.c0sq - (double)o0[u] / a.c0sq;
-                  red_b += dr * dr;
-                }
+                const float dn = gs[i0 + u] - o0[u];
+                red_a = fmaf(dn, dn, red_a);
               }
             }
             store4<NP, VW>(r0, i0, o0);
@@ -573,7 +569,10 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
     // residual components: 0 p, 1 p/c0^2, 2.. velocity components
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      double v = !row_ok ? 0.0 : (c == 0 ? (q == 0 ? red_a : 0.0) : c == 1 ? red_b : (q == c - 1 ? red_a : 0.0));
+      const double ra = (double)red_a;
+      double v = !row_ok ? 0.0
+                         : (c == 0 ? (q == 0 ? ra : 0.0)
+                                   : c == 1 ? (q == 0 ? ra / (a.c0sq * a.c0sq) : 0.0) : (q == c - 1 ? ra : 0.0));
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
       if (lane == 0) sRed[warp * 5 + c] = v;
