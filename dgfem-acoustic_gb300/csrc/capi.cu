@@ -121,23 +121,16 @@ template <typename T>
 __global__ void k_euler_commit(T* u, const T* y, const T* snap, int64_t n, int64_t stride, int nv, double c0sq,
                                double* partials) {
   __shared__ double sh[32][5];
-  double red[5] = {0, 0, 0, 0, 0};
+  dgk::ResAcc<T> racc;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     int q = (int)(i / stride);
     T un = y[i];
     u[i] = un;
-    double dn = (double)snap[i] - (double)un;
-    if (q == 0) {
-      red[0] += dn * dn;
-      double dr = (double)snap[i] / c0sq - (double)un / c0sq;
-      red[1] += dr * dr;
-    } else {
-      red[1 + q] += dn * dn;
-    }
+    racc.add(q, snap[i], un, c0sq);
   }
   const int tid = threadIdx.x;
   for (int c = 0; c < 5; ++c) {
-    double v = red[c];
+    double v = racc.get(c, c0sq);
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
     if ((tid & 31) == 0) sh[tid >> 5][c] = v;
   }
