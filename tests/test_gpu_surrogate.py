@@ -3,10 +3,10 @@ query), on a small configuration (10 x 10 grid meshes, 400 RK4 steps, 600
 training runs) so that DG data generation and training take seconds.
 
 What the network gains: it answers queries at >= 100x the rate of the DG
-runs it replaces (timed at the shipped DG configuration), it predicts held-out spectra better than the best constant
-guess (the mean training spectrum), and its fallback hands every query whose
-estimated error is above the bound back to DG, whose answers it returns
-unchanged."""
+runs it replaces (timed at the shipped DG configuration), it predicts
+held-out spectra better than the best constant guess (the mean training
+spectrum), and its fallback hands every query whose estimated error is above
+the bound back to DG, whose answers it returns unchanged."""
 import time
 
 import numpy as np
