@@ -227,21 +227,47 @@ class Surrogate:
         return mean, from_dg, est
 
     def save(self, path):
-        np.savez_compressed(path, params=np.stack([n.get_params() for n in self.nets]), mu=self.mu,
-                            sigma=self.sigma, scale=self.scale, widths=np.array(WIDTHS), grid=self.grid,
-                            steps=self.steps)
+        """Weights as their BF16 values (what the forward pass uses, so a
+        loaded surrogate answers exactly as this one), biases and the
+        normalisation in FP32."""
+        params = np.stack([n.get_params() for n in self.nets])
+        wmask = _weight_mask(WIDTHS)
+        w16 = (_bf16_bits(params[:, wmask]) >> 16).astype(np.uint16)
+        np.savez_compressed(path, weights_bf16=w16, biases=params[:, ~wmask], mu=self.mu, sigma=self.sigma,
+                            scale=self.scale, widths=np.array(WIDTHS), grid=self.grid, steps=self.steps)
 
     @classmethod
     def load(cls, path, device=0):
         d = np.load(path)
         if list(d["widths"]) != WIDTHS:
             raise ValueError("network widths in %s differ from %s" % (path, WIDTHS))
-        return cls(list(d["params"]), d["mu"], float(d["sigma"]), float(d["scale"]), int(d["grid"]), int(d["steps"]),
+        wmask = _weight_mask(WIDTHS)
+        w16, b = d["weights_bf16"], d["biases"]
+        params = np.zeros((w16.shape[0], wmask.size), dtype=np.float32)
+        params[:, wmask] = (w16.astype(np.uint32) << 16).view(np.float32)
+        params[:, ~wmask] = b
+        return cls(list(params), d["mu"], float(d["sigma"]), float(d["scale"]), int(d["grid"]), int(d["steps"]),
                    device=device)
 
     def close(self):
         for n in self.nets:
             n.close()
+
+
+def _weight_mask(widths):
+    """True at the weight entries of the flat parameter vector (False at the
+    biases)."""
+    m = []
+    for k, n in zip(widths[:-1], widths[1:]):
+        m += [np.ones(n * k, dtype=bool), np.zeros(n, dtype=bool)]
+    return np.concatenate(m)
+
+
+def _bf16_bits(x):
+    """uint32 bit patterns of float32 values rounded to BF16 (ties to even),
+    as the GPU rounds its master weights."""
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
 
 
 def _init(widths, seed):
