@@ -246,10 +246,19 @@ def run_ensemble(args):
 
     dofs = sum(i["mesh"]["elem_nodes"].size * 3 for i in insts)
     B = make(pkg.gpu.DG_FP32, insts)
+    fused = B.fused
     B.run(args.warmup)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         ms = B.bench(args.steps)
     batched = dofs / (ms * 1e-3)
+    # the other way of running the same batch, for comparison
+    alt = None
+    if fused:
+        B.set_fused(False)
+        B.run(args.warmup)
+        ms_graph = B.bench(args.steps)
+        alt = {"mode": "one stage kernel per element order (parallel graph branches)", "ms_per_step": ms_graph,
+               "dof_updates_per_s": dofs / (ms_graph * 1e-3)}
     B.close()
     peak, peak_kind = measured_peak_gbs()
     rec_bytes = geometry_record_words(2, 4) * 4 + 8 * 4
@@ -313,6 +322,9 @@ def run_ensemble(args):
             "plain_single_instance": {"value": plain, "unit": UNIT, "sample": "%d instances run one by one"
                                       % len(sample)},
             "batched_over_plain": batched / plain,
+            "launch": "one persistent launch per RK stage for all orders (work queue)" if fused else
+                      "one stage kernel per element order (parallel graph branches)",
+            "other_launch_mode": alt,
             "roofline": {"bound": "hbm", "achieved": all_bytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": all_bytes / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_step": int(all_bytes), "time": "whole step (graph)"},

@@ -7,25 +7,33 @@
 //
 // Instances of one element type (dim, order) are concatenated into one
 // disjoint-union mesh and solved by one context whose geometry records carry
-// each element's own mean flow and time step. Every step is one CUDA graph:
-// the per-type contexts run their source injection, four fused RK4 stages
-// and observer reductions on their own streams as parallel branches of the
-// graph.
+// each element's own mean flow and time step. Every step is one CUDA graph.
+// For 2-D FP32 instances of orders 2-4 (the ensemble study) every RK stage of
+// all instances is one persistent launch of the mixed-order stage kernel
+// (stage_multi.cuh), whose blocks take tiles of every order from a work
+// queue; otherwise the per-type contexts run their source injection, four
+// fused RK4 stages and observer reductions on their own streams as parallel
+// branches of the graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
 #include <vector>
 
 #include "ctx.h"
+#include "dg_internal.cuh"
 
 namespace dgc {
 int create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, const double* elem_v0,
                const double* elem_scale, dg_ctx** out, std::string* err);
 cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev);
+cudaError_t enqueue_inject(dg_ctx* c);
+cudaError_t enqueue_finalize(dg_ctx* c, int nparts);
+dgk::StageArgs<float> stage_args_f32(dg_ctx* c, int stage, const float* y_in, float* y_out, double dt);
 int ensure_out_cap(dg_ctx* c, int64_t n);
 void set_global_error(const std::string& m);
 }  // namespace dgc
@@ -60,6 +68,13 @@ struct dg_batch {
   cudaStream_t main = nullptr;
   cudaEvent_t fork = nullptr;
   cudaGraphExec_t graph = nullptr;
+  // one launch per RK stage for all element orders (2-D FP32, orders 2-4):
+  // slot k -> group holding order k + 2 (or -1), the four stages' work-queue
+  // counters, the launch's grid
+  bool fused_ok = false, fused = false;
+  int slot_group[dgk::kMultiOrders] = {-1, -1, -1};
+  unsigned* d_queue = nullptr;
+  int fused_grid = 0;
   int64_t step = 0, total_dofs = 0;
   std::string err;
 };
@@ -136,6 +151,53 @@ int sync_inputs(dg_batch* b) {
   return DG_OK;
 }
 
+// One graph per step with one launch per RK stage for every element order:
+// queue counters reset, per-order source injection, the four mixed-order
+// stage kernels, per-order residual and observer reductions (all on the
+// batch's stream; the group contexts' work is enqueued there).
+int build_fused_graph(dg_batch* b) {
+  cudaGraph_t graph = nullptr;
+  BCK(b, cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaMemsetAsync(b->d_queue, 0, 4 * sizeof(unsigned), b->main);
+  std::vector<cudaStream_t> keep;
+  for (auto& g : b->groups) keep.push_back(g.ctx->stream), g.ctx->stream = b->main;
+  for (auto& g : b->groups)
+    if (err == cudaSuccess) err = dgc::enqueue_inject(g.ctx);
+  int* derr = nullptr;
+  for (int st = 1; st <= 4 && err == cudaSuccess; ++st) {
+    dgk::MultiArgs m{};
+    m.ntiles_total = 0;
+    m.queue = b->d_queue + (st - 1);
+    for (int k = 0; k < dgk::kMultiOrders; ++k) {
+      m.g[k].stage = st;
+      m.g[k].ntiles = 0;
+      if (b->slot_group[k] < 0) continue;
+      dg_ctx* c = b->groups[b->slot_group[k]].ctx;
+      const float* in[4] = {(const float*)c->u, (const float*)c->y0, (const float*)c->y1, (const float*)c->y0};
+      float* out[4] = {(float*)c->y0, (float*)c->y1, (float*)c->y0, nullptr};
+      // every instance's own dt sits in its elements' step scale
+      m.g[k] = dgc::stage_args_f32(c, st, in[st - 1], out[st - 1], 1.0);
+      m.g[k].ntiles = (int)(c->Epad / dgk::stage_multi_elems_per_tile(k + 2));
+      m.ntiles_total += m.g[k].ntiles;
+      if (!derr) derr = c->d_err;
+    }
+    err = dgk::launch_stage_multi(m, b->fused_grid, derr, b->main);
+  }
+  for (auto& g : b->groups)
+    if (err == cudaSuccess) err = dgc::enqueue_finalize(g.ctx, b->fused_grid);
+  for (size_t i = 0; i < b->groups.size(); ++i) b->groups[i].ctx->stream = keep[i];
+  cudaError_t err2 = cudaStreamEndCapture(b->main, &graph);
+  if (err != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(b, DG_ERR_CUDA, std::string("CUDA (capture): ") + cudaGetErrorString(err));
+  }
+  BCK(b, err2);
+  err = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  BCK(b, err);
+  return DG_OK;
+}
+
 // One graph per step: every group's step as a parallel branch.
 int build_graph(dg_batch* b, int64_t n_steps) {
   for (auto& g : b->groups) {
@@ -143,6 +205,7 @@ int build_graph(dg_batch* b, int64_t n_steps) {
     if (rc) return fail(b, rc, dg_last_error(g.ctx));
   }
   if (b->graph) return DG_OK;
+  if (b->fused) return build_fused_graph(b);
   cudaGraph_t graph = nullptr;
   BCK(b, cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaEventRecord(b->fork, b->main);
@@ -267,6 +330,31 @@ int dg_batch_create(int n, const dg_mesh_desc* meshes, const dg_phys* phys, cons
   if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
     return bail(DG_ERR_CUDA, "stream/event creation failed");
+  // one launch per stage for all orders: 2-D FP32 instances of orders 2-4
+  b->fused_ok = precision == DG_FP32;
+  for (size_t k = 0; k < b->groups.size(); ++k) {
+    const auto& g = b->groups[k];
+    if (g.dim != 2 || g.order < 2 || g.order > 4)
+      b->fused_ok = false;
+    else
+      b->slot_group[g.order - 2] = (int)k;
+  }
+  if (b->fused_ok) {
+    const int bps = dgk::stage_multi_blocks_per_sm();
+    int64_t tiles = 0;
+    int cap = 1 << 30;
+    for (auto& g : b->groups) {
+      tiles += g.ctx->Epad / dgk::stage_multi_elems_per_tile(g.order);
+      cap = std::min(cap, g.ctx->max_grid);  // rows of every order's partial-sum array
+    }
+    b->fused_grid = (int)std::min<int64_t>(std::min<int64_t>(tiles, (int64_t)bps * b->groups[0].ctx->num_sms), cap);
+    if (bps <= 0 || b->fused_grid <= 0 || cudaMalloc(&b->d_queue, 4 * sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      b->fused_ok = false;
+    }
+  }
+  const char* ev = std::getenv("DGFEM_BATCH_FUSED");
+  b->fused = b->fused_ok && !(ev && std::strcmp(ev, "0") == 0);
   *out = b;
   return DG_OK;
 }
@@ -280,9 +368,23 @@ int dg_batch_destroy(dg_batch* b) {
   }
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->main) cudaStreamDestroy(b->main);
+  if (b->d_queue) cudaFree(b->d_queue);
   delete b;
   return DG_OK;
 }
+
+int dg_batch_set_fused(dg_batch* b, int on) {
+  if (!b) return DG_ERR_ARG;
+  if (on && !b->fused_ok)
+    return fail(b, DG_ERR_ARG, "one launch per stage needs FP32 2-D instances of orders 2-4 only");
+  if (b->fused != (on != 0)) {
+    b->fused = on != 0;
+    if (b->graph) cudaGraphExecDestroy(b->graph), b->graph = nullptr;
+  }
+  return DG_OK;
+}
+
+int dg_batch_fused(const dg_batch* b) { return b && b->fused ? 1 : 0; }
 
 int dg_batch_info(const dg_batch* b, int* n_groups, int64_t* total_dofs) {
   if (!b) return DG_ERR_ARG;

@@ -182,7 +182,7 @@ int fail(dg_ctx* c, int code, const std::string& msg) {
   } while (0)
 
 template <typename T>
-cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_out, double dt) {
+dgk::StageArgs<T> stage_args(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_out, double dt) {
   dgk::StageArgs<T> a{};
   a.y_in = y_in;
   a.y_out = y_out;
@@ -204,6 +204,12 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   a.dt = dt;
   a.c0sq = c->c0sq;
   a.ph = c->ph;
+  return a;
+}
+
+template <typename T>
+cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_out, double dt) {
+  const dgk::StageArgs<T> a = stage_args<T>(c, stage, y_in, y_out, k_out, dt);
   if (c->variant == dgk::kTcVariant) {
     if constexpr (sizeof(T) == 4) return dgk::launch_stage_tc(c->dim, c->order, a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
@@ -234,11 +240,8 @@ cudaError_t launch_stage(dg_ctx* c, int stage, const void* y_in, void* y_out, vo
   return launch_stage_t<double>(c, stage, (const double*)y_in, (double*)y_out, (double*)k_out, dt);
 }
 
-// One time step on c->stream. kind 0: RK4, 1: Euler1. ev (optional, 8
-// events) brackets the stage launches for kernel timing.
-cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
-  cudaError_t err;
-  const int64_t stride = c->Epad * c->np;
+// Source overwrite before a step (k_inject on c->stream).
+cudaError_t enqueue_inject(dg_ctx* c) {
   if (c->n_src_dofs > 0) {
     if (c->prec == DG_FP32)
       k_inject<float><<<nblk(c->n_src_dofs, 128), 128, 0, c->stream>>>(
@@ -248,8 +251,37 @@ cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
       k_inject<double><<<nblk(c->n_src_dofs, 128), 128, 0, c->stream>>>(
           (double*)c->u, c->d_src_dof, c->d_src_off, c->d_src_ids, c->d_srcval, c->n_src, c->srcval_steps, c->d_step,
           c->n_src_dofs);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    return cudaGetLastError();
   }
+  return cudaSuccess;
+}
+
+// Residual means (from nparts rows of stage-4 partial sums) and observer
+// samples after a step, then the step counter (on c->stream).
+cudaError_t enqueue_finalize(dg_ctx* c, int nparts) {
+  const int64_t stride = c->Epad * c->np;
+  double inv_count = 1.0 / (double)(c->E * c->np);
+  if (c->prec == DG_FP32)
+    k_finalize<float><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res, (const float*)c->u,
+                                                          stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w,
+                                                          c->d_obs, c->n_obs, c->d_step, c->out_cap);
+  else
+    k_finalize<double><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res,
+                                                           (const double*)c->u, stride, c->nv, c->d_obs_dof,
+                                                           c->d_obs_off, c->d_obs_w, c->d_obs, c->n_obs, c->d_step,
+                                                           c->out_cap);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  k_advance<<<1, 1, 0, c->stream>>>(c->d_step);
+  return cudaGetLastError();
+}
+
+// One time step on c->stream. kind 0: RK4, 1: Euler1. ev (optional, 8
+// events) brackets the stage launches for kernel timing.
+cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
+  cudaError_t err;
+  const int64_t stride = c->Epad * c->np;
+  if ((err = enqueue_inject(c)) != cudaSuccess) return err;
   int nparts = c->variant >= 0 ? c->grid2 : c->grid;
   if (kind == 0) {
     const void* in[4] = {c->u, c->y0, c->y1, c->y0};
@@ -274,19 +306,7 @@ cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) {
                                                         n, stride, c->nv, c->c0sq, c->partials);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
-  double inv_count = 1.0 / (double)(c->E * c->np);
-  if (c->prec == DG_FP32)
-    k_finalize<float><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res, (const float*)c->u,
-                                                          stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w,
-                                                          c->d_obs, c->n_obs, c->d_step, c->out_cap);
-  else
-    k_finalize<double><<<1 + c->n_obs, 256, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res,
-                                                           (const double*)c->u, stride, c->nv, c->d_obs_dof,
-                                                           c->d_obs_off, c->d_obs_w, c->d_obs, c->n_obs, c->d_step,
-                                                           c->out_cap);
-  if ((err = cudaGetLastError()) != cudaSuccess) return err;
-  k_advance<<<1, 1, 0, c->stream>>>(c->d_step);
-  return cudaGetLastError();
+  return enqueue_finalize(c, nparts);
 }
 
 int ensure_out_cap(dg_ctx* c, int64_t n) {
@@ -485,6 +505,11 @@ int select_variant(dg_ctx* c, int want) {
 namespace dgc {
 void set_global_error(const std::string& m) { g_create_error = m; }
 cudaError_t enqueue_step(dg_ctx* c, int kind, double dt, cudaEvent_t* ev) { return ::enqueue_step(c, kind, dt, ev); }
+cudaError_t enqueue_inject(dg_ctx* c) { return ::enqueue_inject(c); }
+cudaError_t enqueue_finalize(dg_ctx* c, int nparts) { return ::enqueue_finalize(c, nparts); }
+dgk::StageArgs<float> stage_args_f32(dg_ctx* c, int stage, const float* y_in, float* y_out, double dt) {
+  return ::stage_args<float>(c, stage, y_in, y_out, nullptr, dt);
+}
 int ensure_out_cap(dg_ctx* c, int64_t n) { return ::ensure_out_cap(c, n); }
 int create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, const double* elem_v0,
                const double* elem_scale, dg_ctx** out, std::string* err);

@@ -166,6 +166,20 @@ cudaError_t stage3_upload_ops(int dim, int order, const float* Dt, const float* 
 cudaError_t launch_stage3(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,
                           cudaStream_t s);
 Stage2Info stage3_info(int dim, int order, int variant);
+// Mixed-order stage kernel of the batched ensemble (stage_multi.cuh): 2-D,
+// FP32, orders 2-4, one launch per RK stage over every order's tiles.
+// Per-launch description: one StageArgs per order slot (slot k holds order
+// k + 2; ntiles 0 for an order the batch does not hold, stage set in every
+// slot) and the work-queue counter of the launch (zero when it starts).
+constexpr int kMultiOrders = 3;
+struct MultiArgs {
+  StageArgs<float> g[kMultiOrders];
+  int ntiles_total;
+  unsigned* queue;
+};
+int stage_multi_elems_per_tile(int order);
+int stage_multi_blocks_per_sm();
+cudaError_t launch_stage_multi(const MultiArgs& m, int grid, int* err, cudaStream_t s);
 // element padding: every tile size divides this
 constexpr int kElemAlign = 128;
 

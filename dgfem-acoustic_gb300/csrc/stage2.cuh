@@ -271,11 +271,179 @@ struct Pipe {
   static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
 };
 
+// One tile of the pipelined stage for elements e0 .. e0+ET-1: neighbour
+// gathers, volume term, face fluxes, lift and the RK update. The tile's stage
+// input and geometry records (sY, sGF, sGI) have arrived; its RK operands sE
+// (u, accumulator, snapshot: nepi of them) arrive on bar_epi with phase parity
+// epi_parity. The caller synchronises the block before the buffers are reused.
+template <class C, typename T>
+__device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* sY, const T* sGF, const int* sGI,
+                                          const T* sE, T* sN, const T* sD, const T* sL, const short* sFm,
+                                          const short* sNb, uint64_t* bar_epi, uint32_t epi_parity, int nepi, int tid,
+                                          bool& ok, ResAcc<T>& racc) {
+  constexpr int D = C::D, NP = C::NP, NV = C::NV, NK = C::NK;
+  constexpr int NC = C::NC, NSPLIT = C::NSPLIT, ET = C::ET, RECF = C::RECF;
+  const int stage = a.stage;
+  const int64_t stride = a.stride;
+  const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
+  const T dt = (T)a.dt;
+  const int e = tid / NSPLIT, s = tid - (tid / NSPLIT) * NSPLIT;
+  const int i0 = s * NC;
+  // ---- neighbour traces: asynchronous gathers into sN ----
+  gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
+  cp_async_commit();
+
+  // ---- volume term for this thread's nodes ----
+  T Lv[NC][NV];
+  {
+    T W[D][NC][NV];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+      for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) W[r][ii][q] = 0;
+    const T* ye = sY + e * NP;
+#pragma unroll 4
+    for (int j = 0; j < NP; ++j) {
+      T yq[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        T dv[NC];
+        load_chunk<T, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
+#pragma unroll
+        for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) W[r][ii][q] += dv[ii] * yq[q];
+      }
+    }
+    const T* G = sGF + e * RECF;
+    T g[D][D];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+      for (int d = 0; d < D; ++d) g[r][d] = G[r * D + d];
+    const T* ev0 = G + C::S::PHYS_OFF;
+    T gv0[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      gv0[r] = g[r][0] * ev0[0] + g[r][1] * ev0[1];
+      if (D == 3) gv0[r] += g[r][2] * ev0[2];
+    }
+#pragma unroll
+    for (int ii = 0; ii < NC; ++ii) {
+      T vp = 0, vv[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) vv[d] = 0;
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        T gw = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) gw += g[r][d] * W[r][ii][1 + d];
+        vp += gv0[r] * W[r][ii][0] + rhoc2 * gw;
+#pragma unroll
+        for (int d = 0; d < D; ++d) vv[d] += gv0[r] * W[r][ii][1 + d] + g[r][d] * W[r][ii][0] * inv_rho0;
+      }
+      Lv[ii][0] = vp;
+#pragma unroll
+      for (int d = 0; d < D; ++d) Lv[ii][1 + d] = vv[d];
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  // ---- face numerical fluxes (in place of the gathered traces) ----
+  face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
+  __syncthreads();
+
+  // ---- lifting ----
+  {
+    const T* hrow = sN + (size_t)e * C::NKP;
+#pragma unroll 4
+    for (int k = 0; k < NK; ++k) {
+      T hq[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) hq[q] = hrow[(size_t)q * ET * C::NKP + k];
+      T lv[NC];
+      load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
+#pragma unroll
+      for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv[ii] * hq[q];
+    }
+  }
+
+  // ---- RK update from registers (vectorised when the node chunk allows) ----
+  if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity)) ok = false;
+  const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
+  const T* ea = sE + (size_t)NV * ET * NP;
+  const T* es = sE + (size_t)2 * NV * ET * NP;
+  constexpr int VW = C::VW;
+  const T dte = dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+#pragma unroll
+    for (int c0 = 0; c0 < NC; c0 += VW) {
+      const int i = i0 + c0;
+      if (i >= NP) continue;
+      const int lidx = (q * ET + e) * NP + i;
+      const int64_t g = q * stride + (e0 + e) * NP + i;
+      T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
+#pragma unroll
+      for (int v = 0; v < VW; ++v) kv[v] = dte * Lv[c0 + v][q];
+      switch (stage) {
+        case 0:
+          vstore<T, VW>(a.k_out + g, kv);
+          break;
+        case 1:
+          vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) o1[v] = kv[v], o2[v] = xu[v] + (T)0.5 * kv[v];
+          vstore<T, VW>(a.acc + g, o1);
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+        case 2:
+        case 3:
+          vload<T, VW>(xu, eu + lidx);
+          vload<T, VW>(xa, ea + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v)
+            o1[v] = xa[v] + (T)2 * kv[v], o2[v] = xu[v] + (stage == 2 ? (T)0.5 * kv[v] : kv[v]);
+          vstore<T, VW>(a.acc + g, o1);
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+        case 4: {
+          T xs[VW];
+          vload<T, VW>(xu, eu + lidx);
+          vload<T, VW>(xa, ea + lidx);
+          vload<T, VW>(xs, es + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) {
+            const T un = xu[v] + (xa[v] + kv[v]) / (T)6;
+            o1[v] = un;
+            racc.add(q, xs[v], un, a.c0sq);
+          }
+          vstore<T, VW>(a.u + g, o1);
+          break;
+        }
+        default:
+          vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) o2[v] = xu[v] + kv[v];
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+      }
+    }
+  }
+}
+
 template <typename T, int D, int P, int NC_, int ET_>
 __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(const StageArgs<T> a, int* err) {
   using C = Pipe<T, D, P, NC_, ET_>;
   constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
-  constexpr int NC = C::NC, NSPLIT = C::NSPLIT, ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
+  constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
   extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::oBar);  // [0],[1]: tile buffers, [2]: epilogue operands
   T* sD = reinterpret_cast<T*>(sm + C::oD);
@@ -328,12 +496,8 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
   __syncthreads();
   if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0);
 
-  const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
-  const T dt = (T)a.dt;
   ResAcc<T> racc;
   bool ok = true;
-  const int e = tid / NSPLIT, s = tid - (tid / NSPLIT) * NSPLIT;
-  const int i0 = s * NC;
 
   int it = 0;
   for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
@@ -349,154 +513,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       if (nt < a.ntiles) issue_tile(nt, b ^ 1);
       if (nepi > 0) issue_epi(tile);
     }
-    // ---- neighbour traces: asynchronous gathers into sN ----
-    gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
-    cp_async_commit();
-
-    // ---- volume term for this thread's nodes ----
-    T Lv[NC][NV];
-    {
-      T W[D][NC][NV];
-#pragma unroll
-      for (int r = 0; r < D; ++r)
-#pragma unroll
-        for (int ii = 0; ii < NC; ++ii)
-#pragma unroll
-          for (int q = 0; q < NV; ++q) W[r][ii][q] = 0;
-      const T* ye = sY + e * NP;
-#pragma unroll 4
-      for (int j = 0; j < NP; ++j) {
-        T yq[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-          T dv[NC];
-          load_chunk<T, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
-#pragma unroll
-          for (int ii = 0; ii < NC; ++ii)
-#pragma unroll
-            for (int q = 0; q < NV; ++q) W[r][ii][q] += dv[ii] * yq[q];
-        }
-      }
-      const T* G = sGF + e * RECF;
-      T g[D][D];
-#pragma unroll
-      for (int r = 0; r < D; ++r)
-#pragma unroll
-        for (int d = 0; d < D; ++d) g[r][d] = G[r * D + d];
-      const T* ev0 = G + C::S::PHYS_OFF;
-      T gv0[D];
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        gv0[r] = g[r][0] * ev0[0] + g[r][1] * ev0[1];
-        if (D == 3) gv0[r] += g[r][2] * ev0[2];
-      }
-#pragma unroll
-      for (int ii = 0; ii < NC; ++ii) {
-        T vp = 0, vv[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) vv[d] = 0;
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-          T gw = 0;
-#pragma unroll
-          for (int d = 0; d < D; ++d) gw += g[r][d] * W[r][ii][1 + d];
-          vp += gv0[r] * W[r][ii][0] + rhoc2 * gw;
-#pragma unroll
-          for (int d = 0; d < D; ++d) vv[d] += gv0[r] * W[r][ii][1 + d] + g[r][d] * W[r][ii][0] * inv_rho0;
-        }
-        Lv[ii][0] = vp;
-#pragma unroll
-        for (int d = 0; d < D; ++d) Lv[ii][1 + d] = vv[d];
-      }
-    }
-    cp_async_wait_all();
-    __syncthreads();
-
-    // ---- face numerical fluxes (in place of the gathered traces) ----
-    face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
-    __syncthreads();
-
-    // ---- lifting ----
-    {
-      const T* hrow = sN + (size_t)e * C::NKP;
-#pragma unroll 4
-      for (int k = 0; k < NK; ++k) {
-        T hq[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) hq[q] = hrow[(size_t)q * ET * C::NKP + k];
-        T lv[NC];
-        load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
-#pragma unroll
-        for (int ii = 0; ii < NC; ++ii)
-#pragma unroll
-          for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv[ii] * hq[q];
-      }
-    }
-
-    // ---- RK update from registers (vectorised when the node chunk allows) ----
-    if (nepi > 0 && ok && !mbar_wait(&bar[2], it & 1)) ok = false;
-    const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
-    const T* ea = sE + (size_t)NV * ET * NP;
-    const T* es = sE + (size_t)2 * NV * ET * NP;
-    constexpr int VW = C::VW;
-    const T dte = dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
-#pragma unroll
-    for (int q = 0; q < NV; ++q) {
-#pragma unroll
-      for (int c0 = 0; c0 < NC; c0 += VW) {
-        const int i = i0 + c0;
-        if (i >= NP) continue;
-        const int lidx = (q * ET + e) * NP + i;
-        const int64_t g = q * stride + (e0 + e) * NP + i;
-        T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
-#pragma unroll
-        for (int v = 0; v < VW; ++v) kv[v] = dte * Lv[c0 + v][q];
-        switch (stage) {
-          case 0:
-            vstore<T, VW>(a.k_out + g, kv);
-            break;
-          case 1:
-            vload<T, VW>(xu, eu + lidx);
-#pragma unroll
-            for (int v = 0; v < VW; ++v) o1[v] = kv[v], o2[v] = xu[v] + (T)0.5 * kv[v];
-            vstore<T, VW>(a.acc + g, o1);
-            vstore<T, VW>(a.y_out + g, o2);
-            break;
-          case 2:
-          case 3:
-            vload<T, VW>(xu, eu + lidx);
-            vload<T, VW>(xa, ea + lidx);
-#pragma unroll
-            for (int v = 0; v < VW; ++v)
-              o1[v] = xa[v] + (T)2 * kv[v], o2[v] = xu[v] + (stage == 2 ? (T)0.5 * kv[v] : kv[v]);
-            vstore<T, VW>(a.acc + g, o1);
-            vstore<T, VW>(a.y_out + g, o2);
-            break;
-          case 4: {
-            T xs[VW];
-            vload<T, VW>(xu, eu + lidx);
-            vload<T, VW>(xa, ea + lidx);
-            vload<T, VW>(xs, es + lidx);
-#pragma unroll
-            for (int v = 0; v < VW; ++v) {
-              const T un = xu[v] + (xa[v] + kv[v]) / (T)6;
-              o1[v] = un;
-              racc.add(q, xs[v], un, a.c0sq);
-            }
-            vstore<T, VW>(a.u + g, o1);
-            break;
-          }
-          default:
-            vload<T, VW>(xu, eu + lidx);
-#pragma unroll
-            for (int v = 0; v < VW; ++v) o2[v] = xu[v] + kv[v];
-            vstore<T, VW>(a.y_out + g, o2);
-            break;
-        }
-      }
-    }
+    pipe_tile<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     __syncthreads();  // buffers of this tile are free again
   }
   if (!ok) atomicOr(err, 1);

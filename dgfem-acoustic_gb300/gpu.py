@@ -21,7 +21,8 @@ SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_st
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
            "dg_bench_steps", "dg_tune", "dg_kernel_info", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
-           "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench",
+           "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench", "dg_batch_set_fused",
+           "dg_batch_fused",
            "dg_mlp_create", "dg_mlp_destroy", "dg_mlp_last_error", "dg_mlp_param_count", "dg_mlp_set_params",
            "dg_mlp_get_params", "dg_mlp_forward", "dg_mlp_forward_device", "dg_mlp_gradient", "dg_mlp_set_data",
            "dg_mlp_train"]
@@ -261,6 +262,8 @@ def _batch_lib():
     L.dg_batch_set_observers.argtypes = [C.c_void_p, C.c_int, C.c_int, P(I64), P(I64), P(D)]
     L.dg_batch_run.argtypes = [C.c_void_p, I64, P(D)]
     L.dg_batch_bench.argtypes = [C.c_void_p, I64, P(D)]
+    L.dg_batch_set_fused.argtypes = [C.c_void_p, C.c_int]
+    L.dg_batch_fused.argtypes = [C.c_void_p]
     L._batch = True
     return L
 
@@ -360,6 +363,15 @@ class Batch:
             out.append(buf[pos:pos + n_steps * k * 4].reshape(n_steps, k, 4))
             pos += n_steps * k * 4
         return out
+
+    def set_fused(self, on):
+        """One launch per RK stage for all element orders (FP32 2-D orders
+        2-4) when on, else one stage kernel per order."""
+        self._ck(_batch_lib().dg_batch_set_fused(self.h, 1 if on else 0), "dg_batch_set_fused")
+
+    @property
+    def fused(self):
+        return bool(_batch_lib().dg_batch_fused(self.h))
 
     def bench(self, n_steps):
         ms = C.c_double()
