@@ -60,9 +60,11 @@ def test_fused_matches_per_order_graph_and_fp64(pkg, orders):
     s_g, o_g, used_g = _run(pkg, insts, nsteps, pkg.gpu.DG_FP32, False)
     s_64, o_64, _ = _run(pkg, insts, nsteps, pkg.gpu.DG_FP64, None)
     assert used_f and not used_g
+    # both FP32 paths (different kernels, different rounding) within the FP32
+    # bound of the FP64 batch and of each other
     for k in range(len(insts)):
-        assert rel_l2(s_f[k][:3], s_g[k][:3]) <= 1e-6, (k, rel_l2(s_f[k][:3], s_g[k][:3]))
-        assert rel_l2(s_f[k][:3], s_64[k][:3]) <= 1e-5, k
+        assert rel_l2(s_f[k][:3], s_g[k][:3]) <= 1e-5, (k, rel_l2(s_f[k][:3], s_g[k][:3]))
+        assert rel_l2(s_f[k][:3], s_64[k][:3]) <= 1e-5, (k, rel_l2(s_f[k][:3], s_64[k][:3]))
         ok = np.isfinite(o_64[k])
         assert np.array_equal(np.isfinite(o_f[k]), ok)
         assert rel_l2(o_f[k][ok], o_64[k][ok]) <= 1e-4, k
