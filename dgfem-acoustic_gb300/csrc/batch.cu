@@ -353,8 +353,11 @@ int dg_batch_create(int n, const dg_mesh_desc* meshes, const dg_phys* phys, cons
       b->fused_ok = false;
     }
   }
+  // one kernel per order stays the default (measured faster on the
+  // 256-instance ensemble); DGFEM_BATCH_FUSED=1 or dg_batch_set_fused selects
+  // one launch per stage
   const char* ev = std::getenv("DGFEM_BATCH_FUSED");
-  b->fused = b->fused_ok && !(ev && std::strcmp(ev, "0") == 0);
+  b->fused = b->fused_ok && ev && std::strcmp(ev, "1") == 0;
   *out = b;
   return DG_OK;
 }

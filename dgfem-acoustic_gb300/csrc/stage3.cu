@@ -20,7 +20,7 @@ struct V3 {
   X(2, 4, 5, 2) X(2, 4, 5, 1) X(2, 4, 8, 2)                 \
   X(3, 1, 4, 2) X(3, 1, 2, 2)                               \
   X(3, 2, 5, 2) X(3, 2, 5, 1)                               \
-  X(3, 3, 5, 1) X(3, 3, 10, 1) X(3, 3, 7, 1)                \
+  X(3, 3, 5, 1) X(3, 3, 5, 2) X(3, 3, 7, 1)                 \
   X(3, 4, 5, 1) X(3, 4, 7, 1)
 
 std::mutex g_mu;

@@ -58,7 +58,7 @@ struct C3Cfg {
   static constexpr int NT = 32 * EG * NSPLIT;
   static constexpr int RECF = S::RECF, RECI = S::RECI;
   static constexpr int NKP = NK | 1;
-  static constexpr bool UNROLL = NP <= 20;  // compile-time operator addresses
+  static constexpr bool UNROLL = NP <= 16;  // compile-time operator addresses
   static constexpr int OFF_DT = COpsOff<D_, P>::v, OFF_L = OFF_DT + D * NP * NP;
   static constexpr uint32_t YSEG = ET * NP * sizeof(float);
   static constexpr uint32_t GFB = ET * RECF * sizeof(float);

@@ -7,7 +7,7 @@
 // and run each tile with the pipelined kernel's per-tile code for that order
 // (pipe_tile in stage2.cuh), at 128 threads per block for every order:
 //   p = 2: 64 elements per tile, 3 nodes per thread;
-//   p = 3: 64 elements per tile, 5 nodes per thread;
+//   p = 3: 32 elements per tile, 3 nodes per thread;
 //   p = 4: 32 elements per tile, 4 nodes per thread.
 // Every order's reference operators sit in shared memory. The tile buffers
 // are two fixed slots sized for the largest order (consecutive queue items
@@ -24,7 +24,7 @@
 namespace dgk {
 
 using MultiC2 = Pipe<float, 2, 2, 3, 64>;
-using MultiC3 = Pipe<float, 2, 3, 5, 64>;
+using MultiC3 = Pipe<float, 2, 3, 3, 32>;
 using MultiC4 = Pipe<float, 2, 4, 4, 32>;
 constexpr int kMultiNT = 128;
 
