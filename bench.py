@@ -222,7 +222,7 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "setup_ms": info["setup_ms"],
         "kernel_variant": info["kernel_variant"], "kernel_grid": info["kernel_grid"],
-        "kernel_variants": {str(v): S.kernel_info(v) for v in [-1] + list(range(8)) + [16] if S.kernel_info(v)[0] > 0},
+        "kernel_variants": {str(v): S.kernel_info(v) for v in [-1] + list(range(8)) + [16, 17] + list(range(32, 40)) if S.kernel_info(v)[0] > 0},
     }
     S.close()
     return line

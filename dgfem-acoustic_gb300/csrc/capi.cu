@@ -210,8 +210,9 @@ dgk::StageArgs<T> stage_args(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k
 template <typename T>
 cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_out, double dt) {
   const dgk::StageArgs<T> a = stage_args<T>(c, stage, y_in, y_out, k_out, dt);
-  if (c->variant == dgk::kTcVariant) {
-    if constexpr (sizeof(T) == 4) return dgk::launch_stage_tc(c->dim, c->order, a, c->grid2, c->d_err, c->stream);
+  if (dgk::is_tc_variant(c->variant)) {
+    if constexpr (sizeof(T) == 4)
+      return dgk::launch_stage_tc(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
   }
   if (c->variant >= dgk::kStage3Variant) {
@@ -388,15 +389,16 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
   if (v >= dgk::kStage3Variant)
     return c->prec == DG_FP32 ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
                               : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
-  if (v == dgk::kTcVariant)
-    return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order) : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
+  if (dgk::is_tc_variant(v))
+    return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order, dgk::tc_npart(v))
+                              : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (c->prec == DG_FP32) return c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v) : dgk::stage2_info_f32_3d(c->order, v);
   return c->dim == 2 ? dgk::stage2_info_f64_2d(c->order, v) : dgk::stage2_info_f64_3d(c->order, v);
 }
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
-// kTcVariant the tensor-core kernel, kStage3Variant + k constant-operator
-// variant k (both FP32).
+// kTcVariant and kTcVariant + 1 the tensor-core kernels, kStage3Variant + k
+// constant-operator variant k (all three FP32).
 bool set_variant(dg_ctx* c, int v) {
   if (v < 0) {
     c->variant = -1;
@@ -439,9 +441,9 @@ int select_variant(dg_ctx* c, int want) {
     if (si.nc == 0) break;
     if (si.blocks_per_sm > 0) cands.push_back(v);
   }
-  {
-    dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
-    if (si.nc > 0 && si.blocks_per_sm > 0) cands.push_back(dgk::kTcVariant);
+  for (int v = dgk::kTcVariant; v < dgk::kTcVariant + dgk::kTcVariants; ++v) {
+    dgk::Stage2Info si = stage2_info(c, v);
+    if (si.nc > 0 && si.blocks_per_sm > 0) cands.push_back(v);
   }
   for (int k = 0; k < 8; ++k) {
     dgk::Stage2Info si = stage2_info(c, dgk::kStage3Variant + k);
@@ -694,8 +696,8 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     if (si.nc == 0) break;
     c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
   }
-  {
-    dgk::Stage2Info si = stage2_info(c, dgk::kTcVariant);
+  for (int v = dgk::kTcVariant; v < dgk::kTcVariant + dgk::kTcVariants; ++v) {
+    dgk::Stage2Info si = stage2_info(c, v);
     if (si.nc > 0)
       c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
   }

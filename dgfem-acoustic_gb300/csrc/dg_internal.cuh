@@ -153,11 +153,16 @@ Stage2Info stage2_info_f32_2d(int order, int variant);
 Stage2Info stage2_info_f32_3d(int order, int variant);
 Stage2Info stage2_info_f64_2d(int order, int variant);
 Stage2Info stage2_info_f64_3d(int order, int variant);
-// Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant id
-// kTcVariant of the context's kernel selection.
+// Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant ids
+// kTcVariant (2 threads per tile row, 256 per block) and kTcVariant + 1
+// (4 threads per row, 512 per block) of the context's kernel selection.
 constexpr int kTcVariant = 16;
-cudaError_t launch_stage_tc(int dim, int order, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
-Stage2Info stage_tc_info(int dim, int order);
+constexpr int kTcVariants = 2;
+inline bool is_tc_variant(int v) { return v >= kTcVariant && v < kTcVariant + kTcVariants; }
+inline int tc_npart(int v) { return v == kTcVariant ? 2 : 4; }
+cudaError_t launch_stage_tc(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
+                            cudaStream_t s);
+Stage2Info stage_tc_info(int dim, int order, int npart);
 // Constant-operator stage kernel (stage3.cuh, FP32 state only): variant ids
 // kStage3Variant + k of the context's kernel selection; the operators are
 // uploaded to constant memory once per device and element type.

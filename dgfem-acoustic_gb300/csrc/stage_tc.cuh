@@ -151,7 +151,7 @@ __device__ __forceinline__ void store4(float* row, int j0, const float* v) {
   }
 }
 
-template <int D_, int P>
+template <int D_, int P, int NPART_>
 struct TcCfg {
   using T = float;
   using S = ShapeT<D_, P, float>;
@@ -159,7 +159,8 @@ struct TcCfg {
   static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NV = S::NV, NPERM = S::NPERM, NK = NF * NFP;
   static constexpr int ET = 32;            // elements per tile
   static constexpr int ROWS = NV * ET;     // used rows of the M = 128 tile
-  static constexpr int NT = 256;           // two threads per row (lane quarters x halves)
+  static constexpr int NPART = NPART_;     // threads per row: columns split NPART ways
+  static constexpr int NT = 128 * NPART;   // lane quarters x parts
   static constexpr int RECF = S::RECF, RECI = S::RECI;
   static constexpr int NKP = NK | 1;
   static constexpr int NPP = RoundUpTc<NP, 4>::v;       // volume block width per direction
@@ -202,9 +203,9 @@ struct TcCfg {
   static_assert(bytes <= 227 * 1024, "shared memory of one block exceeds 227 KB");
 };
 
-template <int D, int P>
-__global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageArgs<float> a, int* err) {
-  using C = TcCfg<D, P>;
+template <int D, int P, int NPART>
+__global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const StageArgs<float> a, int* err) {
+  using C = TcCfg<D, P, NPART>;
   using T = float;
   constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
   constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, NPP = C::NPP, KV = C::KV, KF = C::KF, KT = C::KT;
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
   double* sRed = reinterpret_cast<double*>(sm + C::oR);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int lq = warp & 3, half = warp >> 2;  // tensor-memory lane quarter, column half
+  const int lq = warp & 3, part = warp >> 2;  // tensor-memory lane quarter, column part
   const int m = lq * 32 + lane;               // tile row = (q, e)
   const bool row_ok = lq * 32 < C::ROWS;      // warp-uniform
   const int q = m / ET, e = m - (m / ET) * ET;
@@ -297,12 +298,12 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
   {
     const uint32_t z[4] = {0u, 0u, 0u, 0u};
     if (row_ok) {
-      for (int c = KV + KF + 4 * half; c < KT; c += 8) {
+      for (int c = KV + KF + 4 * part; c < KT; c += 4 * NPART) {
         tmem_st4(trow + C::COL_AH + c, z);
         tmem_st4(trow + C::COL_AL + c, z);
       }
     } else {
-      for (int c = 4 * half; c < KT; c += 8) {
+      for (int c = 4 * part; c < KT; c += 4 * NPART) {
         tmem_st4(trow + C::COL_AH + c, z);
         tmem_st4(trow + C::COL_AL + c, z);
       }
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
         if (D == 3) gv0[r] += g[r][2] * v0[2];
       }
       const T* ye = sY + e * NP;
-      for (int g4 = half; g4 < NPP / 4; g4 += 2) {
+      for (int g4 = part; g4 < NPP / 4; g4 += NPART) {
         const int j0 = g4 * 4;
         T yp[4], yv[D][4];
         // p and the velocity components this row needs (all of them for the
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
     // ---- face rows: A_face[(q,e)][k] -> tensor memory ----
     if (row_ok) {
       const T* hrow = sN + (size_t)(q * ET + e) * C::NKP;
-      for (int c4 = half; c4 < KF / 4; c4 += 2) {
+      for (int c4 = part; c4 < KF / 4; c4 += NPART) {
         T x[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) x[u] = (c4 * 4 + u < NK) ? hrow[c4 * 4 + u] : (T)0;
@@ -474,7 +475,7 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
       T* r1 = sE + (size_t)(NV * ET + q * ET + e) * NP;        // slot 1 row: acc in, new acc out
       const T* ry = sY + (size_t)(q * ET + e) * NP;            // stage input row (u in stages 1, 5)
       const T* gs = a.snap + q * stride + (e0 + e) * NP;      // residual snapshot row (stage 4)
-      for (int c4 = half; c4 < NN / 4; c4 += 2) {
+      for (int c4 = part; c4 < NN / 4; c4 += NPART) {
         const int i0 = c4 * 4;
         if (i0 >= NP) break;  // warp-uniform
         float dv[4];
@@ -586,11 +587,11 @@ __global__ void __launch_bounds__(TcCfg<D, P>::NT) stage_tc_kernel(const StageAr
   }
 }
 
-template <int D, int P>
+template <int D, int P, int NPART>
 struct StageTc {
-  using C = TcCfg<D, P>;
+  using C = TcCfg<D, P, NPART>;
   static int blocks_per_sm() {
-    auto kfn = stage_tc_kernel<D, P>;
+    auto kfn = stage_tc_kernel<D, P, NPART>;
     // the largest shared-memory carve-out, so that the occupancy query and
     // the launches see the same per-SM capacity
     if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes) != cudaSuccess ||
@@ -624,7 +625,7 @@ struct StageTc {
     return nb > 0 ? nb : 0;
   }
   static cudaError_t launch(const StageArgs<float>& a, int grid, int* err, cudaStream_t s) {
-    auto kfn = stage_tc_kernel<D, P>;
+    auto kfn = stage_tc_kernel<D, P, NPART>;
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);

@@ -1,7 +1,9 @@
 """The tensor-core stage kernel (tcgen05, 3xTF32 split, FP32 state) and the
 Euler1 integrator against the CPU oracle, through the C ABI.
 
-The tensor-core kernel is kernel variant 16 of an FP32 context. Its products
+The tensor-core kernel is kernel variant 16 (256 threads per block) or 17
+(512 threads per block, each tile row's columns split four ways) of an FP32
+context. Its products
 keep about 21 mantissa bits (x = tf32 head + fp32 tail, the tail-tail product
 dropped), so it is held to the same bounds as the CUDA-core FP32 kernels: a
 single right-hand side within the FP32 single-RHS bound of the oracle and
@@ -16,6 +18,7 @@ from test_gpu_parity import _mesh, _phys, _sources_observers
 pytestmark = pytest.mark.gpu
 
 TC = 16
+TC4 = 17
 
 
 def _obs_err(tr, ref_obs):
@@ -30,9 +33,10 @@ def _solver(pkg, mesh, ph, prec="fp32"):
     return pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
 
 
+@pytest.mark.parametrize("tc", [TC, TC4])
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
-def test_tc_rhs_matches_oracle(pkg, oracle, dim, p):
+def test_tc_rhs_matches_oracle(pkg, oracle, dim, p, tc):
     mesh = _mesh(pkg, dim, p)
     ph = _phys(dim)
     u = smooth_state(mesh, seed=dim * 10 + p)
@@ -42,7 +46,7 @@ def test_tc_rhs_matches_oracle(pkg, oracle, dim, p):
     nv = dim + 1
     assert S.tune(0) == 0
     err_cc = rel_l2(S.rhs(u, dt)[:nv], ref[:nv])
-    assert S.tune(TC) == TC
+    assert S.tune(tc) == tc
     k = S.rhs(u, dt)
     err_tc = rel_l2(k[:nv], ref[:nv])
     assert err_tc <= 5e-4, (dim, p, err_tc)
@@ -54,8 +58,9 @@ def test_tc_rhs_matches_oracle(pkg, oracle, dim, p):
 def test_tc_not_offered_in_fp64(pkg):
     mesh = _mesh(pkg, 2, 2)
     S = _solver(pkg, mesh, _phys(2), "fp64")
-    with pytest.raises(pkg.gpu.SolverError):
-        S.tune(TC)
+    for tc in (TC, TC4):
+        with pytest.raises(pkg.gpu.SolverError):
+            S.tune(tc)
 
 
 def _run(pkg, oracle, mesh, ph, prec, variant, nsteps, euler=False):
@@ -91,10 +96,11 @@ def _run(pkg, oracle, mesh, ph, prec, variant, nsteps, euler=False):
     return S.get_state(), np.concatenate(res), np.concatenate(tr), ref
 
 
-@pytest.mark.parametrize("dim,p", [(2, 2), (2, 3), (2, 4), (3, 2), (3, 3), (3, 4)])
-def test_tc_run_matches_oracle(pkg, oracle, dim, p):
+@pytest.mark.parametrize("dim,p,tc", [(2, 2, TC), (2, 3, TC), (2, 4, TC), (3, 2, TC), (3, 3, TC), (3, 4, TC),
+                                      (2, 3, TC4), (3, 3, TC4)])
+def test_tc_run_matches_oracle(pkg, oracle, dim, p, tc):
     mesh = _mesh(pkg, dim, p)
-    u, res, tr, ref = _run(pkg, oracle, mesh, _phys(dim), "fp32", TC, 40)
+    u, res, tr, ref = _run(pkg, oracle, mesh, _phys(dim), "fp32", tc, 40)
     nv = dim + 1
     assert rel_l2(u[:nv], ref["state"][:nv]) <= 1e-5
     assert rel_l2(res[:, :4], ref["residuals"][:, :4]) <= 1e-3
@@ -113,7 +119,8 @@ def test_euler_run_matches_oracle(pkg, oracle, dim, p, prec, variant):
     assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= tol * 10
 
 
-def test_tc_many_tiles_per_block(pkg, oracle):
+@pytest.mark.parametrize("tc", [TC, TC4])
+def test_tc_many_tiles_per_block(pkg, oracle, tc):
     """A mesh with more tiles than resident blocks, so that every block walks
     several tiles through both halves of its double buffer: one RHS against
     the oracle and 20 RK4 steps against the CUDA-core FP32 kernel."""
@@ -127,10 +134,10 @@ def test_tc_many_tiles_per_block(pkg, oracle):
     dt = 2e-5
     ref = oracle.Problem(mesh, dt=dt, **ph).stage(u0)
     S = _solver(pkg, mesh, ph)
-    assert S.tune(TC) == TC
+    assert S.tune(tc) == tc
     assert rel_l2(S.rhs(u0, dt)[:4], ref[:4]) <= 5e-4
     out = []
-    for v in (1, TC):
+    for v in (1, tc):
         S.tune(v)
         S.set_state(u0)
         S.snapshot()
