@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <cstdio>
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -426,14 +428,99 @@ bool set_variant(dg_ctx* c, int v) {
   return true;
 }
 
+// Autotuner results, cached per (GPU model, dimension, order, precision,
+// mesh size class): in the process, and in the file named by
+// DGFEM_TUNE_CACHE when it is set (one "key<TAB>variant" line per result;
+// a later line for the same key wins).
+struct TuneCache {
+  std::mutex mu;
+  std::map<std::string, int> entries;
+  std::map<std::string, bool> files_read;
+  int64_t hits = 0, misses = 0;
+};
+TuneCache& tune_cache() {
+  static TuneCache tc;
+  return tc;
+}
+
+std::string tune_key(const dg_ctx* c) {
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) {
+    cudaGetLastError();
+    return std::string();
+  }
+  int size_class = 0;
+  while (size_class < 62 && ((int64_t)1 << (size_class + 1)) <= c->Epad) ++size_class;
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s|cc%d.%d|sm%d|d%d|p%d|%s|e2^%d", prop.name, prop.major, prop.minor,
+                prop.multiProcessorCount, c->dim, c->order, c->prec == DG_FP32 ? "fp32" : "fp64", size_class);
+  for (char* q = buf; *q; ++q)
+    if (*q == '\t' || *q == '\n') *q = ' ';
+  return buf;
+}
+
+// caller holds the cache lock
+void tune_cache_read_file(TuneCache& tc, const char* path) {
+  if (!path || !*path || tc.files_read[path]) return;
+  tc.files_read[path] = true;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  char line[768];
+  while (std::fgets(line, sizeof(line), f)) {
+    char* tab = std::strrchr(line, '\t');
+    if (!tab) continue;
+    *tab = 0;
+    char* end = nullptr;
+    long v = std::strtol(tab + 1, &end, 10);
+    if (end == tab + 1) continue;
+    tc.entries[line] = (int)v;
+  }
+  std::fclose(f);
+}
+
+bool tune_cache_lookup(const std::string& key, int* v) {
+  if (key.empty()) return false;
+  TuneCache& tc = tune_cache();
+  std::lock_guard<std::mutex> lk(tc.mu);
+  tune_cache_read_file(tc, std::getenv("DGFEM_TUNE_CACHE"));
+  auto it = tc.entries.find(key);
+  if (it == tc.entries.end()) {
+    ++tc.misses;
+    return false;
+  }
+  ++tc.hits;
+  *v = it->second;
+  return true;
+}
+
+void tune_cache_store(const std::string& key, int v) {
+  if (key.empty()) return;
+  TuneCache& tc = tune_cache();
+  std::lock_guard<std::mutex> lk(tc.mu);
+  tc.entries[key] = v;
+  const char* path = std::getenv("DGFEM_TUNE_CACHE");
+  if (!path || !*path) return;
+  if (FILE* f = std::fopen(path, "a")) {
+    std::fprintf(f, "%s\t%d\n", key.c_str(), v);
+    std::fclose(f);
+  }
+}
+
 // Autotuner: times RK stages 1-3 (stage input, u and accumulator reads;
 // accumulator and next-stage writes) of every kernel variant on this mesh
-// and keeps the fastest. want >= -1 forces
-// a variant instead.
+// and keeps the fastest. want >= -1 forces a variant instead; want == -3
+// takes a cached result for this GPU model, element type, precision and mesh
+// size class where one exists (what context creation does) and times the
+// variants otherwise; want == -2 always times them. Timed results are cached.
 int select_variant(dg_ctx* c, int want) {
   if (want >= -1) {
     if (!set_variant(c, want)) return fail(c, DG_ERR_ARG, "stage kernel variant not available");
     return DG_OK;
+  }
+  const std::string key = tune_key(c);
+  if (want == -3) {
+    int v = -1;
+    if (tune_cache_lookup(key, &v) && set_variant(c, v)) return DG_OK;
   }
   std::vector<int> cands{-1};
   for (int v = 0; v < 8; ++v) {
@@ -499,6 +586,7 @@ int select_variant(dg_ctx* c, int want) {
   cudaMemsetAsync(c->y1, 0, nb, c->stream);
   cudaStreamSynchronize(c->stream);
   set_variant(c, best_v);
+  tune_cache_store(key, best_v);
   return DG_OK;
 }
 
@@ -733,9 +821,9 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     // DGFEM_STAGE_VARIANT forces a kernel where it exists for this context
     // (e.g. the tensor-core kernel only for FP32); elsewhere the autotuner picks
     const char* ev = std::getenv("DGFEM_STAGE_VARIANT");
-    int want = ev ? std::atoi(ev) : -2;
+    int want = ev ? std::atoi(ev) : -3;
     int rc2 = select_variant(c, want);
-    if (rc2 == DG_ERR_ARG && ev) rc2 = select_variant(c, -2);
+    if (rc2 == DG_ERR_ARG && ev) rc2 = select_variant(c, -3);
     if (rc2 != DG_OK) {
       std::string m = c->err;
       dg_destroy(c);
@@ -1000,8 +1088,25 @@ int dg_kernel_info(dg_ctx* c, int variant, int* out) {
   return DG_OK;
 }
 
+int dg_tune_cache_stats(int64_t* hits, int64_t* misses, int64_t* entries) {
+  TuneCache& tc = tune_cache();
+  std::lock_guard<std::mutex> lk(tc.mu);
+  if (hits) *hits = tc.hits;
+  if (misses) *misses = tc.misses;
+  if (entries) *entries = (int64_t)tc.entries.size();
+  return DG_OK;
+}
+
+void dg_tune_cache_clear(void) {
+  TuneCache& tc = tune_cache();
+  std::lock_guard<std::mutex> lk(tc.mu);
+  tc.entries.clear();
+  tc.files_read.clear();
+  tc.hits = tc.misses = 0;
+}
+
 int dg_tune(dg_ctx* c, int variant) {
-  if (!c) return DG_ERR_ARG;
+  if (!c || variant < -3) return DG_ERR_ARG;
   int rc = select_variant(c, variant);
   c->info.kernel_variant = c->variant;
   c->info.kernel_grid = c->variant >= 0 ? c->grid2 : c->grid;

@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_kernel_info", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
+           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_kernel_info", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
            "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench", "dg_batch_set_fused",
            "dg_batch_fused",
@@ -77,6 +77,9 @@ def lib():
         L.dg_stream.restype = C.c_void_p
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
         L.dg_tune.argtypes = [C.c_void_p, C.c_int]
+        L.dg_tune_cache_stats.argtypes = [P(I64), P(I64), P(I64)]
+        L.dg_tune_cache_clear.argtypes = []
+        L.dg_tune_cache_clear.restype = None
         L.dg_kernel_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
         L.dg_residuals_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, I64, I64, D, C.c_void_p,
                                            C.c_void_p]
@@ -102,6 +105,18 @@ def _csr(lists, dtype=np.int64):
 
 class SolverError(RuntimeError):
     pass
+
+
+def tune_cache_stats():
+    """(hits, misses, entries) of the autotuner's process-wide result cache."""
+    h, m, n = C.c_int64(), C.c_int64(), C.c_int64()
+    lib().dg_tune_cache_stats(C.byref(h), C.byref(m), C.byref(n))
+    return h.value, m.value, n.value
+
+
+def tune_cache_clear():
+    """Forgets the cache's in-process entries and counters."""
+    lib().dg_tune_cache_clear()
 
 
 def residuals_noalloc(u_ptr, snap_ptr, precision, n_var, n_per_var, var_stride, c0, res_ptr, stream=None):
@@ -233,6 +248,9 @@ class Solver:
         return tuple(out)
 
     def tune(self, variant=-2):
+        """-2 times every stage-kernel variant on this mesh and keeps the
+        fastest, -3 takes a cached result where one exists, -1 / k >= 0 force
+        the baseline or variant k."""
         self._ck(lib().dg_tune(self.h, variant), "dg_tune")
         return self.info()["kernel_variant"]
 

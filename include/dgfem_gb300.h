@@ -131,8 +131,10 @@ int dg_cell_means(dg_ctx* ctx, double* p, double* rho, double* v);
 int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
 
 /* Stage kernel selection. variant -2: time every variant on this mesh and
- * keep the fastest (what dg_create does; the environment variable
- * DGFEM_STAGE_VARIANT overrides it there); -1: baseline kernel; k >= 0:
+ * keep the fastest; -3: the same, unless the tune cache holds a result for
+ * this GPU model, element type, precision and mesh size class (what
+ * dg_create does; the environment variable DGFEM_STAGE_VARIANT overrides it
+ * there); -1: baseline kernel; k >= 0:
  * pipelined variant k (TMA-staged tiles; the variants differ in output nodes
  * per thread and elements per tile); 16 and 17: tensor-core kernel with 256
  * or 512 threads per block (FP32 contexts only: tcgen05 MMAs with a 3xTF32
@@ -141,6 +143,17 @@ int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
  * DG_ERR_ARG for a variant that does not exist for this element type or
  * precision. */
 int dg_tune(dg_ctx* ctx, int variant);
+
+/* The autotuner's result cache (process-wide; keyed by GPU model, dimension,
+ * order, precision and the mesh's size class floor(log2(padded elements))).
+ * Every timed selection stores its winner; when DGFEM_TUNE_CACHE names a
+ * file, results are also appended to it and read back from it on the first
+ * lookup, so later processes skip the timing. Replaces no reference
+ * interface (the reference has no kernel selection). */
+int dg_tune_cache_stats(int64_t* hits, int64_t* misses, int64_t* entries);
+/* Forgets the in-process entries and counters (the file is left as is and
+ * is read again on the next lookup). */
+void dg_tune_cache_clear(void);
 
 /* Launch shape of stage-kernel variant `variant` (as in dg_tune) for this
  * context: out[0] elements per tile (0: not available), out[1] threads per
