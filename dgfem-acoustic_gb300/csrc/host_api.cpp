@@ -3,9 +3,11 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "quadrature.h"
 #include "../../include/dgfem_host.h"
 #include "config.h"
 #include "host_common.h"
@@ -124,6 +126,23 @@ int dgh_spectra(const float* p, int64_t n, double dt, int64_t* nb, double* fft_r
     dgout::spectra(p, n, dt, nb, f, q);
     if (fft_rows) std::memcpy(fft_rows, f.data(), f.size() * sizeof(double));
     if (psd_rows) std::memcpy(psd_rows, q.data(), q.size() * sizeof(double));
+  });
+}
+
+int dgh_quadrature(int kind, int degree, int* n, double* x, double* w) {
+  return dghost::guard([&] {
+    dgref::QRule r;
+    if (kind == 1)
+      r = dgref::gauss_legendre(degree);
+    else if (kind == 2)
+      r = dgref::triangle_rule(degree);
+    else if (kind == 3)
+      r = dgref::tetrahedron_rule(degree);
+    else
+      throw std::runtime_error("quadrature kind must be 1 (line), 2 (triangle) or 3 (tetrahedron)");
+    *n = r.n;
+    if (x) std::memcpy(x, r.x.data(), r.x.size() * sizeof(double));
+    if (w) std::memcpy(w, r.w.data(), r.w.size() * sizeof(double));
   });
 }
 

@@ -1,5 +1,7 @@
 #include "refelem.h"
 
+#include "quadrature.h"
+
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -322,6 +324,97 @@ RefElement build(int dim, int p) {
         re.LIFT[i * (nf * nfp) + f * nfp + m] = s;
       }
   return re;
+}
+
+CurvedTables build_curved(const RefElement& re) {
+  const int D = re.dim, p = re.p, np = re.np, nf = re.nf, nfp = re.nfp;
+  std::vector<double> nodes(np * D);
+  for (int n = 0; n < np; ++n)
+    for (int d = 0; d < D; ++d) nodes[n * D + d] = (double)re.lattice[n * D + d] / p;
+  const auto ex = monomials(D, p);
+  const auto C = lagrange_coeffs(D, p, nodes, ex);
+  const int nm = (int)ex.size() / D;
+  // phi_j(xi) and d phi_j / d xi_r
+  auto eval = [&](const double* xi, double* phi, double* dphi /* [D][np] */) {
+    std::vector<double> m(nm), dm(D * nm);
+    for (int k = 0; k < nm; ++k) {
+      double v = 1.0;
+      for (int d = 0; d < D; ++d) v *= std::pow(xi[d], ex[k * D + d]);
+      m[k] = v;
+      for (int r = 0; r < D; ++r) {
+        const int a = ex[k * D + r];
+        double g = 0.0;
+        if (a > 0) {
+          g = a * std::pow(xi[r], a - 1);
+          for (int d = 0; d < D; ++d)
+            if (d != r) g *= std::pow(xi[d], ex[k * D + d]);
+        }
+        dm[r * nm + k] = g;
+      }
+    }
+    for (int j = 0; j < np; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < nm; ++k) s += C[k * np + j] * m[k];
+      if (phi) phi[j] = s;
+      for (int r = 0; r < D && dphi; ++r) {
+        double g = 0.0;
+        for (int k = 0; k < nm; ++k) g += C[k * np + j] * dm[r * nm + k];
+        dphi[r * np + j] = g;
+      }
+    }
+  };
+  CurvedTables t;
+  const QRule er = element_rule(D, p), fr = face_rule(D, p);
+  t.ng = er.n, t.ngf = fr.n;
+  t.qw = er.w, t.fw = fr.w;
+  t.qB.assign((size_t)t.ng * np, 0.0);
+  t.qD.assign((size_t)D * t.ng * np, 0.0);
+  std::vector<double> dphi(D * np);
+  for (int g = 0; g < t.ng; ++g) {
+    eval(&er.x[g * D], &t.qB[(size_t)g * np], dphi.data());
+    for (int r = 0; r < D; ++r)
+      for (int j = 0; j < np; ++j) t.qD[((size_t)r * t.ng + g) * np + j] = dphi[r * np + j];
+  }
+  // reference coordinates of the mesh corners: vertex 0 at the origin,
+  // vertex k at the unit vector e_k
+  auto corner = [&](int c, double* xi) {
+    for (int d = 0; d < D; ++d) xi[d] = (c > 0 && d == c - 1) ? 1.0 : 0.0;
+  };
+  t.fB.assign((size_t)nf * t.ngf * nfp, 0.0);
+  t.fTu.assign((size_t)nf * t.ngf * np, 0.0);
+  if (D == 3) t.fTv.assign((size_t)nf * t.ngf * np, 0.0);
+  std::vector<double> phi(np);
+  for (int lf = 0; lf < nf; ++lf) {
+    double c0[3], c1[3], c2[3] = {0, 0, 0};
+    corner(re.face_corners[lf][0], c0), corner(re.face_corners[lf][1], c1);
+    if (D == 3) corner(re.face_corners[lf][2], c2);
+    double du[3], dv[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      // 2-D: u in [-1, 1] from corner 0 to corner 1; 3-D: (u, v) on the
+      // unit triangle with corners 0, 1, 2 at (0,0), (1,0), (0,1)
+      du[d] = D == 2 ? 0.5 * (c1[d] - c0[d]) : c1[d] - c0[d];
+      if (D == 3) dv[d] = c2[d] - c0[d];
+    }
+    for (int g = 0; g < t.ngf; ++g) {
+      double xi[3];
+      if (D == 2) {
+        const double u = fr.x[g];
+        for (int d = 0; d < D; ++d) xi[d] = c0[d] * 0.5 * (1.0 - u) + c1[d] * 0.5 * (1.0 + u);
+      } else {
+        const double u = fr.x[g * 2], v = fr.x[g * 2 + 1];
+        for (int d = 0; d < D; ++d) xi[d] = c0[d] * (1.0 - u - v) + c1[d] * u + c2[d] * v;
+      }
+      eval(xi, phi.data(), dphi.data());
+      for (int m = 0; m < nfp; ++m) t.fB[((size_t)lf * t.ngf + g) * nfp + m] = phi[re.fmask[lf * nfp + m]];
+      for (int j = 0; j < np; ++j) {
+        double a = 0.0, b = 0.0;
+        for (int r = 0; r < D; ++r) a += dphi[r * np + j] * du[r], b += dphi[r * np + j] * dv[r];
+        t.fTu[((size_t)lf * t.ngf + g) * np + j] = a;
+        if (D == 3) t.fTv[((size_t)lf * t.ngf + g) * np + j] = b;
+      }
+    }
+  }
+  return t;
 }
 
 }  // namespace dgref

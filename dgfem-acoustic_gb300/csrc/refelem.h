@@ -48,6 +48,24 @@ struct RefElement {
 
 RefElement build(int dim, int p);
 
+// Tables of the curved-element path, which follows the reference's own
+// quadrature formulation element by element (src/Mesh.cpp:40-137 element
+// Jacobians at the quadrature points, :209-260 face points, :691-839 mass,
+// stiffness and face integrals). Internal node order; the face points of
+// local face lf are the face rule's points mapped through that face's corner
+// order (face_corners[lf]).
+struct CurvedTables {
+  int ng = 0, ngf = 0;
+  std::vector<double> qw;   // [ng] element rule weights
+  std::vector<double> qB;   // [ng][np] phi_j at the element points
+  std::vector<double> qD;   // [dim][ng][np] d phi_j / d xi_r at the element points
+  std::vector<double> fw;   // [ngf] face rule weights
+  std::vector<double> fB;   // [nf][ngf][nfp] phi of face node m at the face points
+  std::vector<double> fTu;  // [nf][ngf][np] d phi_j / du along the face parametrization
+  std::vector<double> fTv;  // [nf][ngf][np] d phi_j / dv (3-D; empty in 2-D)
+};
+CurvedTables build_curved(const RefElement& re);
+
 // Internal node index of lattice point (i,j[,k]); -1 if outside.
 int lattice_index(const RefElement& re, const int* ijk);
 

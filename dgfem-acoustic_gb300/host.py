@@ -35,6 +35,8 @@ def lib():
                                      C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.dgh_count_steps.argtypes = [C.c_double] * 4 + [C.POINTER(C.c_int64)] * 2
         L.dgh_schedule.argtypes = [C.c_double] * 4 + [C.POINTER(C.c_double), C.POINTER(C.c_ubyte)]
+        L.dgh_quadrature.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -243,3 +245,19 @@ def write_pvd(path, t_start, t_end, dt, t_rate):
     _setup_more(L)
     if L.dgh_write_pvd(path.encode(), t_start, t_end, dt, t_rate) != 0:
         raise RuntimeError(_err())
+
+
+def quadrature(kind, degree):
+    """The curved-element path's quadrature rule: kind 1 Gauss-Legendre line
+    on [-1, 1] with `degree` points, 2 triangle and 3 tetrahedron rule of that
+    degree; returns (points [n][dim], weights [n])."""
+    L = lib()
+    n = C.c_int()
+    if L.dgh_quadrature(kind, degree, C.byref(n), None, None) != 0:
+        raise RuntimeError(L.dgh_last_error().decode())
+    x = np.zeros(n.value * kind)
+    w = np.zeros(n.value)
+    L.dgh_quadrature(kind, degree, C.byref(n), x.ctypes.data_as(C.POINTER(C.c_double)),
+                     w.ctypes.data_as(C.POINTER(C.c_double)))
+    return x.reshape(n.value, kind), w
+

@@ -103,6 +103,12 @@ void dgh_free(void* p);
 int dgh_write_spectra(const char* prefix, const float* p, int64_t n, double dt);
 /* Amplitude spectrum rows [nb/2][5] (freq, norm, real, imag, SPL) and one-sided
  * PSD rows [nb/2+1][3] (freq, PSD, dB) of a trace, as written to the files */
+/* Quadrature rules of the curved-element path (stand-ins for Gmsh's
+ * Gauss(2p) rules, src/Mesh.cpp:49-52,213-215): kind 1 Gauss-Legendre line
+ * on [-1,1] with `degree` points, 2 triangle rule of that degree, 3
+ * tetrahedron rule of that degree. *n receives the point count; x (n*dim
+ * reference coordinates) and w (n weights) are filled when non-NULL. */
+int dgh_quadrature(int kind, int degree, int* n, double* x, double* w);
 int dgh_spectra(const float* p, int64_t n, double dt, int64_t* nb, double* fft_rows, double* psd_rows);
 
 #ifdef __cplusplus

@@ -1283,4 +1283,17 @@ int refcpu_run(const refcpu_input* in, refcpu_output* out) {
   }
 }
 
+int refcpu_rule(int kind, int degree, int* n, double* x, double* w) {
+  try {
+    Rule r = kind == 1 ? gauss_line(degree) : kind == 2 ? tri_rule(degree) : tet_rule(degree);
+    *n = r.n;
+    if (x) std::copy(r.x.begin(), r.x.end(), x);
+    if (w) std::copy(r.w.begin(), r.w.end(), w);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
 }  // extern "C"

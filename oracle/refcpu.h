@@ -118,6 +118,10 @@ int refcpu_faces(const refcpu_input* in, int64_t* face_id, int64_t* nbr, int* or
 /* Initial state from the Gaussian ICs (src/dgalerkin.cpp:51-70). u: [4][E*Np] */
 int refcpu_initial_state(const refcpu_input* in, double* u);
 
+/* The oracle's stand-in quadrature rules: kind 1 Gauss line with `degree`
+ * points, 2 triangle rule, 3 tetrahedron rule of that degree. */
+int refcpu_rule(int kind, int degree, int* n, double* x, double* w);
+
 const char* refcpu_last_error(void);
 
 #ifdef __cplusplus

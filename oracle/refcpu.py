@@ -58,6 +58,8 @@ def lib():
                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.refcpu_initial_state.argtypes = [C.POINTER(Input), C.POINTER(C.c_double)]
         L.refcpu_count_steps.argtypes = [C.c_double] * 4 + [C.POINTER(C.c_int64)] * 2
+        L.refcpu_rule.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
         L.refcpu_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -178,3 +180,18 @@ class Problem:
         sh = (E, nf)
         return dict(face_id=fid.reshape(sh), nbr=nbr.reshape(sh), orient=orient.reshape(sh),
                     bc=bc.reshape(sh), penalty=pen.reshape(sh))
+
+
+def rule(kind, degree):
+    """The oracle's quadrature rule: kind 1 Gauss line (degree = points),
+    2 triangle, 3 tetrahedron; returns (points [n][dim], weights [n])."""
+    L = lib()
+    n = C.c_int()
+    if L.refcpu_rule(kind, degree, C.byref(n), None, None) != 0:
+        raise RuntimeError(L.refcpu_last_error().decode())
+    dim = {1: 1, 2: 2, 3: 3}[kind]
+    x = np.zeros(n.value * dim)
+    w = np.zeros(n.value)
+    L.refcpu_rule(kind, degree, C.byref(n), _p(x, C.c_double), _p(w, C.c_double))
+    return x.reshape(n.value, dim), w
+
