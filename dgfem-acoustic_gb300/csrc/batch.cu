@@ -334,7 +334,7 @@ int dg_batch_create(int n, const dg_mesh_desc* meshes, const dg_phys* phys, cons
   b->fused_ok = precision == DG_FP32;
   for (size_t k = 0; k < b->groups.size(); ++k) {
     const auto& g = b->groups[k];
-    if (g.dim != 2 || g.order < 2 || g.order > 4)
+    if (g.dim != 2 || g.order < 2 || g.order > 4 || g.ctx->ncurved > 0)
       b->fused_ok = false;
     else
       b->slot_group[g.order - 2] = (int)k;
@@ -379,7 +379,7 @@ int dg_batch_destroy(dg_batch* b) {
 int dg_batch_set_fused(dg_batch* b, int on) {
   if (!b) return DG_ERR_ARG;
   if (on && !b->fused_ok)
-    return fail(b, DG_ERR_ARG, "one launch per stage needs FP32 2-D instances of orders 2-4 only");
+    return fail(b, DG_ERR_ARG, "one launch per stage needs FP32 2-D straight-sided instances of orders 2-4 only");
   if (b->fused != (on != 0)) {
     b->fused = on != 0;
     if (b->graph) cudaGraphExecDestroy(b->graph), b->graph = nullptr;

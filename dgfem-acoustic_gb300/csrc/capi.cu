@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "ctx.h"
+#include "curved.cuh"
 
 namespace {
 
@@ -198,6 +199,9 @@ dgk::StageArgs<T> stage_args(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k
   a.bmat = (const T*)c->bmat;
   a.Dt = (const T*)c->Dt;
   a.LIFT = (const T*)c->LIFT;
+  a.cslot = c->ncurved > 0 ? c->cslot : nullptr;
+  a.crhs = (const T*)c->crhs;
+  a.cstride = c->ncurved * c->np;
   a.fmask = c->fmask;
   a.nbrnode = c->nbrnode;
   a.stride = c->Epad * c->np;
@@ -239,6 +243,11 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
 }
 
 cudaError_t launch_stage(dg_ctx* c, int stage, const void* y_in, void* y_out, void* k_out, double dt) {
+  // curved elements first: their right-hand side from the same stage input
+  if (c->ncurved > 0) {
+    cudaError_t e = dgc::launch_curved(c, y_in);
+    if (e != cudaSuccess) return e;
+  }
   if (c->prec == DG_FP32) return launch_stage_t<float>(c, stage, (const float*)y_in, (float*)y_out, (float*)k_out, dt);
   return launch_stage_t<double>(c, stage, (const double*)y_in, (double*)y_out, (double*)k_out, dt);
 }
@@ -387,6 +396,12 @@ void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>&
 }
 
 
+// The tensor-core and constant-operator kernels have no curved-element
+// path; the baseline and pipelined kernels take the curved right-hand side.
+bool variant_handles_mesh(const dg_ctx* c, int v) {
+  return c->ncurved == 0 || !(dgk::is_tc_variant(v) || v >= dgk::kStage3Variant);
+}
+
 dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
   if (v >= dgk::kStage3Variant)
     return c->prec == DG_FP32 ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
@@ -406,6 +421,7 @@ bool set_variant(dg_ctx* c, int v) {
     c->variant = -1;
     return true;
   }
+  if (!variant_handles_mesh(c, v)) return false;
   dgk::Stage2Info si = stage2_info(c, v);
   if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return false;
   if (v >= dgk::kStage3Variant) {
@@ -814,6 +830,7 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
   cudaEventDestroy(t1);
   c->info.dim = c->dim, c->info.order = c->order, c->info.nodes_per_elem = c->np, c->info.n_var = c->nv;
   c->info.precision = c->prec, c->info.n_elems = c->E, c->info.n_faces = c->n_faces;
+  c->info.n_curved = c->ncurved;
   c->info.n_boundary_faces = c->n_bfaces;
   c->info.device_bytes = c->device_bytes;
   c->info.setup_ms = ms;
@@ -1082,7 +1099,7 @@ int dg_kernel_info(dg_ctx* c, int variant, int* out) {
   }
   dgk::Stage2Info si = stage2_info(c, variant);
   // available exactly when dg_tune accepts it
-  if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return DG_OK;
+  if (!variant_handles_mesh(c, variant) || si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return DG_OK;
   out[0] = si.et, out[1] = si.nt, out[2] = si.smem_bytes, out[3] = si.blocks_per_sm;
   out[4] = (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms);
   return DG_OK;

@@ -64,6 +64,20 @@ struct dg_ctx {
   int64_t* d_obs_dof = nullptr;
   int64_t* d_obs_off = nullptr;
   double* d_obs_w = nullptr;
+  // curved elements (curved.cu): slot table, per-element quadrature data and
+  // the per-stage right-hand side of those elements
+  int64_t ncurved = 0;
+  int cng = 0, cngf = 0;
+  int* cslot = nullptr;      // [Epad] slot of a curved element, -1 otherwise (null: none)
+  int64_t* celem = nullptr;  // [ncurved] element of each slot
+  void* cA = nullptr;        // [ncurved][ng][dim][dim]
+  void* cMinv = nullptr;     // [ncurved][np][np]
+  void* cF = nullptr;        // [ncurved][nf][ngf][dim+1]
+  void* cTB = nullptr;       // [ncurved][nf][6]
+  void* cqB = nullptr;       // [ng][np]
+  void* cqD = nullptr;       // [dim][ng][np]
+  void* cfB = nullptr;       // [nf][ngf][nfp]
+  void* crhs = nullptr;      // [nv][ncurved][np]
   // per-step graph
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0.0;

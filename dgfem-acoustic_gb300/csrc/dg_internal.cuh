@@ -123,12 +123,34 @@ struct StageArgs {
   const short* fmask;   // [NF*NFP]
   const short* nbrnode; // [NF*NPERM*NFP]
   int64_t stride;  // Epad*NP
+  // curved elements: per element its slot in crhs (-1: straight-sided); null
+  // when the mesh has none. crhs [NV][cstride] holds M^-T (S - F) of the
+  // curved elements (curved.cu), computed before the stage kernel runs.
+  const int* cslot;
+  const T* crhs;
+  int64_t cstride;  // ncurved*NP
   int ntiles;
   int stage;       // 0: k only, 1..4: RK4 stages, 5: Euler (y_out = u + k)
   double dt;
   double c0sq;
   Phys ph;
 };
+
+// The stage kernels' operator result Lv of this thread's node chunk is
+// replaced by the curved-element right-hand side where the element is
+// curved.
+template <typename T, int NC, int NV, int NP>
+__device__ __forceinline__ void curved_override(const StageArgs<T>& a, int64_t el, int i0, T (&Lv)[NC][NV]) {
+  if (a.cslot == nullptr) return;
+  const int cs = a.cslot[el];
+  if (cs < 0) return;
+  const T* r = a.crhs + (int64_t)cs * NP;
+#pragma unroll
+  for (int ii = 0; ii < NC; ++ii)
+    if (i0 + ii < NP)
+#pragma unroll
+      for (int q = 0; q < NV; ++q) Lv[ii][q] = r[q * a.cstride + i0 + ii];
+}
 
 // Stage launchers and occupancy queries; defined in stage_{f32,f64}_{2,3}d.cu.
 cudaError_t launch_stage_f32_2d(int order, const StageArgs<float>& a, int grid, cudaStream_t s);

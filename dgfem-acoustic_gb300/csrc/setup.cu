@@ -24,6 +24,7 @@
 #include <stdexcept>
 
 #include "ctx.h"
+#include "curved.cuh"
 
 namespace {
 
@@ -52,8 +53,11 @@ __device__ __forceinline__ const double* elem_v0(const SetupDev& s, int64_t e) {
 __device__ __forceinline__ const double* X(const SetupDev& s, int64_t node) { return s.xyz + 3 * node; }
 
 // Per element: J = [x_k - x_0], det J, G = J^-1, and the lattice check of
-// every element node against the shared node permutation.
-__global__ void k_elem_geom(SetupDev s, double* det, double* G, int* err) {
+// every element node against the shared node permutation. An element whose
+// high-order nodes leave the straight-sided lattice by more than 1e-9 lattice
+// spacings is curved (curved[e] = 1); the node order is still read from the
+// nearest lattice points, up to a quarter spacing away.
+__global__ void k_elem_geom(SetupDev s, double* det, double* G, int* curved, int* err) {
   int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= s.E) return;
   const int D = s.dim;
@@ -88,6 +92,7 @@ __global__ void k_elem_geom(SetupDev s, double* det, double* G, int* err) {
   for (int r = 0; r < D; ++r)
     for (int d = 0; d < D; ++d) G[e * D * D + r * D + d] = Gi[r][d];
   // lattice check: node n must sit at the internal lattice point perm[n]
+  int is_curved = 0;
   for (int n = D + 1; n < s.np; ++n) {
     const double* xn = X(s, en[n]);
     double rel[3] = {0, 0, 0};
@@ -98,7 +103,8 @@ __global__ void k_elem_geom(SetupDev s, double* det, double* G, int* err) {
       double xi = 0.0;
       for (int d = 0; d < D; ++d) xi += Gi[r][d] * rel[d];
       double l = xi * s.order, lr = rint(l);
-      if (fabs(l - lr) > 1e-6) ok = false;
+      if (fabs(l - lr) > 1e-9) is_curved = 1;
+      if (!(fabs(l - lr) <= 0.25)) ok = false;
       lat[r] = (int)lr;
     }
     // internal index of the lattice point (same enumeration as dgref::lattice_index)
@@ -115,9 +121,10 @@ __global__ void k_elem_geom(SetupDev s, double* det, double* G, int* err) {
       for (int jj = 0; jj < lat[1]; ++jj) idx += p - lat[2] - jj + 1;
       idx += lat[0];
     }
-    if (!ok) atomicOr(err, 2);                 // curved / non-affine element
+    if (!ok) atomicOr(err, 2);                 // node too far from any lattice point
     else if (idx != s.perm[n]) atomicOr(err, 4);  // element node order differs from element 0
   }
+  curved[e] = is_curved;
 }
 
 __global__ void k_mark_corners(SetupDev s, int* mark) {
@@ -434,7 +441,8 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh, const double* elem_v0, const 
     // ---- element geometry ----
     double* det = S.alloc<double>(E);
     double* G = S.alloc<double>(E * D * D);
-    k_elem_geom<<<blocks(E, 128), 128, 0, st>>>(sd, det, G, err);
+    int* curved = S.alloc<int>(E);
+    k_elem_geom<<<blocks(E, 128), 128, 0, st>>>(sd, det, G, curved, err);
     SETUP_CK(cudaGetLastError());
     // ---- compact vertex ids ----
     int* mark = S.alloc<int>(N + 1);
@@ -520,7 +528,7 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh, const double* elem_v0, const 
     if (herr) {
       std::string m = "mesh setup failed:";
       if (herr & 1) m += " degenerate element;";
-      if (herr & 2) m += " curved or non-affine element (high-order nodes off the straight-sided lattice);";
+      if (herr & 2) m += " element too distorted (a high-order node more than a quarter lattice spacing off its straight-sided position);";
       if (herr & 4) m += " elements do not share one local node ordering;";
       if (herr & 8) m += " face shared by more than two elements;";
       if (herr & 16) m += " face hash table overflow;";
@@ -528,6 +536,9 @@ int run_setup(dg_ctx* c, const dg_mesh_desc* mesh, const double* elem_v0, const 
       c->err = m;
       return DG_ERR_MESH;
     }
+    // ---- curved elements: per-element quadrature data ----
+    int rc = setup_curved(c, xyz, en, perm, det, curved, st);
+    if (rc != DG_OK) return rc;
     return DG_OK;
   } catch (const std::exception& ex) {
     c->err = ex.what();

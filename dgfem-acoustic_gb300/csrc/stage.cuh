@@ -219,6 +219,7 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
         for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv * hq[q];
       }
     }
+    curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
     const T dte = dt * sGF[e * RECF + S::PHYS_OFF + D];  // dt times the element's step scale
     __syncthreads();  // every thread is done reading sY / sH of this tile
 #pragma unroll

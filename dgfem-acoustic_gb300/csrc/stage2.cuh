@@ -375,6 +375,7 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
     }
   }
 
+  curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
   // ---- RK update from registers (vectorised when the node chunk allows) ----
   if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity)) ok = false;
   const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)

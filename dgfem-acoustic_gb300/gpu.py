@@ -44,7 +44,8 @@ class Info(C.Structure):
     _fields_ = [("dim", C.c_int), ("order", C.c_int), ("nodes_per_elem", C.c_int), ("n_var", C.c_int),
                 ("precision", C.c_int), ("n_elems", C.c_int64), ("n_faces", C.c_int64),
                 ("n_boundary_faces", C.c_int64), ("penalty_sign_hist", C.c_int64 * 2),
-                ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("kernel_variant", C.c_int), ("kernel_grid", C.c_int)]
+                ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("kernel_variant", C.c_int), ("kernel_grid", C.c_int),
+                ("n_curved", C.c_int64)]
 
 
 def lib():

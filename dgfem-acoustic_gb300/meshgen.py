@@ -238,3 +238,30 @@ def min_altitude(mesh):
     A = np.max([0.5 * np.linalg.norm(np.cross(P[b] - P[a], P[c] - P[a]), axis=1)
                 for a, b, c in ((0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))], axis=0)
     return float((3 * V / A).min())
+
+
+def warp(mesh, amp, center=None, radius=None):
+    """Copy of a mesh with every node (vertices and high-order nodes) moved by
+    a smooth displacement, which makes the elements it bends curved: the
+    high-order nodes leave the straight-sided lattice of their element's
+    corners. Without a center, a global quadratic bend: x_d += amp *
+    x_{d+1}^2 (cyclic over the mesh's dimensions). With a center and radius, a
+    bump amp * (1 - r^2/R^2)^3 along the diagonal inside the ball of radius R;
+    elements entirely outside it stay straight-sided."""
+    m = dict(mesh)
+    X = np.array(mesh["xyz"], dtype=np.float64)
+    dim = 3 if np.ptp(X[:, 2]) > 0 else 2
+    if center is None:
+        Y = X.copy()
+        for d in range(dim):
+            Y[:, d] += amp * X[:, (d + 1) % dim] ** 2
+    else:
+        c = np.zeros(3)
+        c[:len(center)] = center
+        r2 = np.sum((X - c) ** 2, axis=1) / radius ** 2
+        f = amp * np.clip(1.0 - r2, 0.0, None) ** 3
+        Y = X.copy()
+        for d in range(dim):
+            Y[:, d] += f / np.sqrt(dim)
+    m["xyz"] = Y
+    return m

@@ -52,7 +52,7 @@ enum {
   DG_OK = 0,
   DG_ERR_ARG = 1,       /* invalid argument or call order */
   DG_ERR_CUDA = 2,      /* CUDA runtime error (no device, out of memory, launch failure) */
-  DG_ERR_MESH = 3,      /* unsupported or inconsistent mesh (curved, non-conforming, ...) */
+  DG_ERR_MESH = 3,      /* unsupported or inconsistent mesh (non-conforming, inverted, ...) */
   DG_ERR_NONFINITE = 4, /* NaN/Inf detected in the state */
   DG_ERR_TIMEOUT = 5    /* a bounded device wait gave up */
 };
@@ -92,6 +92,8 @@ typedef struct {
   int kernel_variant; /* stage kernel in use: -1 baseline, 0..15 pipelined variant k, 16/17 tensor-core
                          kernel, 32.. constant-operator variant */
   int kernel_grid;    /* blocks of each stage-kernel launch (persistent blocks for variants >= 0) */
+  int64_t n_curved;   /* curved elements (high-order nodes off the straight-sided lattice), integrated
+                         element by element with the reference's quadrature formulation */
 } dg_info_t;
 
 int dg_create(const dg_mesh_desc* mesh, const dg_phys* phys, int precision, int device, dg_ctx** out);
