@@ -14,10 +14,12 @@
 // reference), 1 on any error (message on stderr).
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <stdexcept>
@@ -42,6 +44,7 @@ void ck(int rc, dg_ctx* c, const char* what) {
 int main(int argc, char** argv) {
   if (argc != 2) return E2BIG;
   dg_ctx* ctx = nullptr;
+  dg_vtu_writer* vw = nullptr;
   try {
     auto wall0 = std::chrono::steady_clock::now();
     dgcfg::Config cfg = dgcfg::load(argv[1]);
@@ -140,9 +143,26 @@ int main(int argc, char** argv) {
                                 : "time;pressure;density;velocity_x;velocity_y;velocity_z\n");
     }
     std::vector<std::vector<float>> wave(no);
-    dgh_mesh* hm = nullptr;
-    if (dgh_mesh_load(cfg.mesh_file.c_str(), &hm) != 0) fail(dgh_last_error());
-    std::vector<double> cp(E), crho(E), cv(3 * E);
+    // VTU snapshots (src/Mesh.cpp:1136-1230): the mesh part once, the cell
+    // means of each output step computed on the GPU and written by the
+    // writer's background thread while the time loop goes on.
+    // DGFEM_VTU_COMPRESSION: 1 zlib (VTK's default), 0 none, unset: zlib when
+    // the system library loads.
+    {
+      int64_t maxtag = 0;
+      for (auto t : mesh.node_tags) maxtag = std::max<int64_t>(maxtag, t);
+      std::vector<double> pts(3 * maxtag, 0.0);
+      for (size_t k = 0; k < mesh.node_tags.size(); ++k)
+        for (int d = 0; d < 3; ++d) pts[3 * (mesh.node_tags[k] - 1) + d] = mesh.xyz[3 * k + d];
+      const int nc = dim + 1;
+      std::vector<int64_t> cells(E * nc);
+      for (int64_t e = 0; e < E; ++e)
+        for (int k = 0; k < nc; ++k) cells[e * nc + k] = mesh.node_tags[mesh.elem_nodes[e * np + k]] - 1;
+      const char* ev = std::getenv("DGFEM_VTU_COMPRESSION");
+      const int comp = ev ? std::atoi(ev) : -1;
+      if (dg_vtu_writer_create(ctx, maxtag, pts.data(), cells.data(), comp, 0, &vw) != DG_OK)
+        fail("cannot create the VTU writer (compression " + std::to_string(comp) + ")");
+    }
     const double c0sq = std::pow(cfg.c0, 2);
     double loop_s = 0.0;
     int64_t i = 0;
@@ -151,9 +171,8 @@ int main(int argc, char** argv) {
       while (j < nsteps && !snap[j]) ++j;
       if (snap[i]) {
         ck(dg_snapshot(ctx), ctx, "dg_snapshot");
-        ck(dg_cell_means(ctx, cp.data(), crho.data(), cv.data()), ctx, "dg_cell_means");
         std::string vtu = "results/result" + std::to_string((int)i) + ".vtu";
-        if (dgh_write_vtu(vtu.c_str(), hm, cp.data(), crho.data(), cv.data()) != 0) fail(dgh_last_error());
+        if (dg_vtu_write_async(vw, vtu.c_str()) != DG_OK) fail(std::string("VTU: ") + dg_vtu_writer_last_error(vw));
         std::printf("[%g/%g s] Step number : %lld\n", times[i], cfg.t_end, (long long)i);
       }
       const int64_t n = j - i;
@@ -187,7 +206,9 @@ int main(int argc, char** argv) {
         fail(dgh_last_error());
     }
     if (dgh_write_pvd("results.pvd", cfg.t_start, cfg.t_end, cfg.dt, cfg.t_rate) != 0) fail(dgh_last_error());
-    dgh_mesh_free(hm);
+    if (dg_vtu_writer_flush(vw) != DG_OK) fail(std::string("VTU: ") + dg_vtu_writer_last_error(vw));
+    dg_vtu_writer_destroy(vw);
+    vw = nullptr;
     double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
     double dofs = (double)E * np * (dim + 1);
     std::printf("Done: %lld steps, time loop %.3f s (%.3e DOF-updates/s), total %.3f s\n", (long long)nsteps, loop_s,
@@ -196,6 +217,7 @@ int main(int argc, char** argv) {
     return 0;
   } catch (const std::exception& e) {
     std::fprintf(stderr, "Error: %s\n", e.what());
+    if (vw) dg_vtu_writer_destroy(vw);
     if (ctx) dg_destroy(ctx);
     return 1;
   }

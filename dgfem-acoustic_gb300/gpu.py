@@ -19,7 +19,8 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_kernel_info", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
+           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_kernel_info", "dg_vtu_writer_create", "dg_vtu_write_async",
+           "dg_vtu_writer_flush", "dg_vtu_writer_destroy", "dg_vtu_writer_last_error", "dg_vtu_writer_stats", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
            "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench", "dg_batch_set_fused",
            "dg_batch_fused",
@@ -79,6 +80,13 @@ def lib():
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
         L.dg_tune.argtypes = [C.c_void_p, C.c_int]
         L.dg_tune_cache_stats.argtypes = [P(I64), P(I64), P(I64)]
+        L.dg_vtu_writer_create.argtypes = [C.c_void_p, I64, P(D), P(I64), C.c_int, C.c_int, P(C.c_void_p)]
+        L.dg_vtu_write_async.argtypes = [C.c_void_p, C.c_char_p]
+        L.dg_vtu_writer_flush.argtypes = [C.c_void_p]
+        L.dg_vtu_writer_destroy.argtypes = [C.c_void_p]
+        L.dg_vtu_writer_last_error.argtypes = [C.c_void_p]
+        L.dg_vtu_writer_last_error.restype = C.c_char_p
+        L.dg_vtu_writer_stats.argtypes = [C.c_void_p, P(I64), P(C.c_int)]
         L.dg_tune_cache_clear.argtypes = []
         L.dg_tune_cache_clear.restype = None
         L.dg_kernel_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
@@ -285,6 +293,48 @@ def _batch_lib():
     L.dg_batch_fused.argtypes = [C.c_void_p]
     L._batch = True
     return L
+
+
+class VtuWriter:
+    """Asynchronous VTU snapshots of a Solver's state (dg_vtu_*): points
+    [n][3] and cells [E][dim+1] (corner point indices) describe the VTK mesh;
+    write(path) returns once the cell means are enqueued on the GPU, a
+    background thread writes the file. compression: 1 zlib, 0 none, -1 zlib
+    when available. Close (or flush) before reading the files."""
+
+    def __init__(self, solver, points, cells, compression=-1, slots=0):
+        L = lib()
+        self.solver = solver
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        cl = np.ascontiguousarray(cells, dtype=np.int64)
+        h = C.c_void_p()
+        rc = L.dg_vtu_writer_create(solver.h, len(pts), _dp(pts), _ip(cl), compression, slots, C.byref(h))
+        if rc != 0:
+            raise SolverError("dg_vtu_writer_create: %s" % ERRORS.get(rc, rc))
+        self.h = h
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise SolverError("%s: %s: %s" % (what, ERRORS.get(rc, rc), lib().dg_vtu_writer_last_error(self.h).decode()))
+
+    def write(self, path):
+        self._ck(lib().dg_vtu_write_async(self.h, str(path).encode()), "dg_vtu_write_async")
+
+    def flush(self):
+        self._ck(lib().dg_vtu_writer_flush(self.h), "dg_vtu_writer_flush")
+
+    def stats(self):
+        """(files written, compressed)"""
+        n, comp = C.c_int64(), C.c_int()
+        lib().dg_vtu_writer_stats(self.h, C.byref(n), C.byref(comp))
+        return n.value, bool(comp.value)
+
+    def close(self):
+        if self.h:
+            rc = lib().dg_vtu_writer_destroy(self.h)
+            self.h = None
+            if rc != 0:
+                raise SolverError("dg_vtu_writer_destroy: %s" % ERRORS.get(rc, rc))
 
 
 class Batch:

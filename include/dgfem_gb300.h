@@ -132,6 +132,28 @@ int dg_cell_means(dg_ctx* ctx, double* p, double* rho, double* v);
  * boundary) and BC code (1 reflecting, 0 absorbing, -1 interior). */
 int dg_face_info(dg_ctx* ctx, int64_t* nbr, int* penalty, int* bc);
 
+/* Asynchronous VTU snapshots (replaces the time loop's synchronous
+ * Mesh::writeVTUb, src/Mesh.cpp:1136-1230, src/solver.cpp:451). A writer
+ * holds the VTK mesh part of every file (points [n_points][3]; cells
+ * [n_elems][dim+1]: the point index of each element corner, the reference's
+ * node tag - 1) and n_slots (0: 3) pinned snapshot slots.
+ * dg_vtu_write_async computes the cell means (p, p/c0^2, velocity; the
+ * reference's formula) of the context's state as of the steps enqueued so
+ * far, on the GPU, and returns; a background thread writes `path` (VTK XML,
+ * appended raw data; compression 1: zlib blocks as VTK's default writer,
+ * 0: uncompressed, -1: zlib when the system library loads). It blocks only
+ * while every slot is in flight. dg_vtu_writer_flush waits for every file
+ * and returns the first failure (message in dg_vtu_writer_last_error).
+ * Destroy the writer before its context. */
+typedef struct dg_vtu_writer dg_vtu_writer;
+int dg_vtu_writer_create(dg_ctx* ctx, int64_t n_points, const double* points, const int64_t* cells, int compression,
+                         int n_slots, dg_vtu_writer** out);
+int dg_vtu_write_async(dg_vtu_writer* w, const char* path);
+int dg_vtu_writer_flush(dg_vtu_writer* w);
+int dg_vtu_writer_destroy(dg_vtu_writer* w);
+const char* dg_vtu_writer_last_error(const dg_vtu_writer* w);
+int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* compressed);
+
 /* Stage kernel selection. variant -2: time every variant on this mesh and
  * keep the fastest; -3: the same, unless the tune cache holds a result for
  * this GPU model, element type, precision and mesh size class (what

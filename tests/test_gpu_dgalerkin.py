@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from vtu_read import read_vtu
 
 pytestmark = pytest.mark.gpu
 
@@ -59,6 +60,16 @@ def test_hilltop_matches_golden_trace(tmp_path):
     res = d / "results"
     for step in range(0, 1000, 100):
         assert (res / ("result%d.vtu" % step)).exists()
+    # snapshots written by the asynchronous writer decode to the mesh's
+    # triangles and finite cell data; the state changes between snapshots
+    v0, v9 = read_vtu(str(res / "result0.vtu")), read_vtu(str(res / "result900.vtu"))
+    for v in (v0, v9):
+        assert v["n_cells"] == len(v["types"]) and np.all(v["types"] == 5)
+        assert v["connectivity"].shape == (3 * v["n_cells"],) and v["connectivity"].max() < v["n_points"]
+        assert np.all(np.isfinite(v["Pressure [Pa]"])) and v["Velocity [m/s]"].shape == (v["n_cells"], 3)
+        scale = np.abs(v["Pressure [Pa]"]).max() / 340.0 ** 2
+        np.testing.assert_allclose(v["Density [kg/m³]"], v["Pressure [Pa]"] / 340.0 ** 2, rtol=0, atol=1e-13 * scale)
+    assert not np.array_equal(v0["Pressure [Pa]"], v9["Pressure [Pa]"])
     pvd = (d / "results.pvd").read_text()
     assert pvd.count("<DataSet") == 10 and 'timestep="0.1" part="0" file="results/result100.vtu"' in pvd
     obs = np.genfromtxt(res / "observers1.txt", delimiter=";", skip_header=1)
