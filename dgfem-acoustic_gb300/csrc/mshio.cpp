@@ -1,10 +1,15 @@
 #include "mshio.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <cstdlib>
+#include <deque>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
+#include <thread>
+#include <type_traits>
 #include <unordered_map>
 
 namespace dgmsh {
@@ -31,28 +36,172 @@ const TypeInfo* find_type(int type) {
   throw std::runtime_error("msh '" + path + "': " + msg);
 }
 
-// Token stream over the whole file (msh ASCII is whitespace separated apart
-// from the quoted names in $PhysicalNames, which are handled line-wise).
+// Token cursor over the whole file held in memory (msh ASCII is whitespace
+// separated apart from the quoted names in $PhysicalNames, which are read
+// line-wise).
+struct WsTable {
+  bool t[256];
+  WsTable() {
+    for (int i = 0; i < 256; ++i) t[i] = i == ' ' || i == '\n' || i == '\r' || i == '\t' || i == '\v' || i == '\f';
+  }
+};
+const WsTable kWs;
+inline bool is_ws(char c) { return kWs.t[(unsigned char)c]; }
+
+// Integer token at p (after whitespace); sets ok = false when there is none.
+inline int64_t parse_int(const char*& p, const char* end, bool& ok) {
+  while (p < end && is_ws(*p)) ++p;
+  bool neg = false;
+  if (p < end && (*p == '-' || *p == '+')) neg = *p == '-', ++p;
+  const char* d0 = p;
+  int64_t v = 0;
+  while (p < end && *p >= '0' && *p <= '9') v = v * 10 + (*p - '0'), ++p;
+  if (p == d0 || (p < end && !is_ws(*p))) {
+    ok = false;
+    return 0;
+  }
+  return neg ? -v : v;
+}
+
+// Floating-point token at p (correctly rounded by strtod; the file buffer
+// ends with a NUL, so strtod cannot run past it).
+inline double parse_double(const char*& p, const char* end, bool& ok) {
+  while (p < end && is_ws(*p)) ++p;
+  char* q = nullptr;
+  const double v = std::strtod(p, &q);
+  if (q == p || (q < end && !is_ws(*q))) {
+    ok = false;
+    return 0.0;
+  }
+  p = q;
+  return v;
+}
+
 struct Reader {
-  std::istream& in;
+  const char* p;
+  const char* end;
   std::string path;
+  bool at_end() {
+    while (p < end && is_ws(*p)) ++p;
+    return p >= end;
+  }
+  std::string token() {
+    while (p < end && is_ws(*p)) ++p;
+    const char* t = p;
+    while (p < end && !is_ws(*p)) ++p;
+    return std::string(t, p);
+  }
   template <class T>
   T get() {
+    bool ok = true;
     T v;
-    if (!(in >> v)) fail(path, "unexpected end of data");
+    if constexpr (std::is_floating_point<T>::value)
+      v = (T)parse_double(p, end, ok);
+    else
+      v = (T)parse_int(p, end, ok);
+    if (!ok) fail(path, at_end() ? "unexpected end of data" : "malformed number '" + token() + "'");
     return v;
   }
   void expect(const std::string& tok) {
-    std::string s;
-    if (!(in >> s) || s != tok) fail(path, "expected '" + tok + "', got '" + s + "'");
+    const std::string s = token();
+    if (s != tok) fail(path, "expected '" + tok + "', got '" + s + "'");
   }
-  void skip_to(const std::string& end) {
-    std::string s;
-    while (in >> s)
-      if (s == end) return;
-    fail(path, "missing " + end);
+  void skip_to(const std::string& end_tok) {
+    while (!at_end())
+      if (token() == end_tok) return;
+    fail(path, "missing " + end_tok);
+  }
+  std::string line() {  // rest of the current line
+    const char* t = p;
+    while (p < end && *p != '\n') ++p;
+    std::string s(t, p);
+    if (p < end) ++p;
+    if (!s.empty() && s.back() == '\r') s.pop_back();
+    return s;
+  }
+  // Skips n tokens; every `every` tokens records where the next one starts.
+  void skip_tokens(int64_t n, int64_t every, std::vector<const char*>& marks) {
+    for (int64_t k = 0; k < n; ++k) {
+      while (p < end && is_ws(*p)) ++p;
+      if (p >= end) fail(path, "unexpected end of data");
+      if (k % every == 0) marks.push_back(p);
+      while (p < end && !is_ws(*p)) ++p;
+    }
   }
 };
+
+// A run of tokens to parse: `n` tokens from `start`, the first being token
+// `first` of its section; `kind` says what they are.
+struct Span {
+  const char* start;
+  int64_t first, n;
+  int kind;       // 0: node tags, 1: node coordinates, 2: 4.0 node records (tag x y z), 3: element records
+  int64_t base;   // first node index (kinds 0-2) or first element of the block (kind 3)
+  int per;        // tokens per element record (kind 3)
+  ElementBlock* blk;
+};
+
+constexpr int64_t kSpan = 1 << 16;  // tokens per parallel task
+
+void parse_spans(const std::vector<Span>& spans, MshFile& f, const std::string& path, const char* end) {
+  std::atomic<size_t> next{0};
+  std::atomic<bool> bad{false};
+  auto work = [&] {
+    for (;;) {
+      const size_t i = next.fetch_add(1);
+      if (i >= spans.size() || bad.load()) return;
+      const Span& s = spans[i];
+      const char* p = s.start;
+      bool ok = true;
+      for (int64_t k = 0; k < s.n && ok; ++k) {
+        const int64_t t = s.first + k;
+        switch (s.kind) {
+          case 0: f.node_tags[s.base + t] = parse_int(p, end, ok); break;
+          case 1: f.node_xyz[3 * s.base + t] = parse_double(p, end, ok); break;
+          case 2: {
+            const int64_t node = s.base + t / 4, c = t % 4;
+            if (c == 0)
+              f.node_tags[node] = parse_int(p, end, ok);
+            else
+              f.node_xyz[3 * node + c - 1] = parse_double(p, end, ok);
+            break;
+          }
+          default: {
+            const int64_t e = t / s.per, c = t % s.per;
+            if (c == 0)
+              s.blk->tags[e] = parse_int(p, end, ok);
+            else
+              s.blk->nodes[e * (s.per - 1) + c - 1] = parse_int(p, end, ok);
+          }
+        }
+      }
+      if (!ok) bad = true;
+    }
+  };
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const unsigned nt = (unsigned)std::min<size_t>(hw, std::max<size_t>(1, spans.size()));
+  if (nt <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+  }
+  if (bad) fail(path, "malformed number in $Nodes or $Elements");
+}
+
+// Records spans of n tokens from the reader's position, then skips them.
+void add_spans(Reader& r, std::vector<Span>& spans, Span proto, int64_t n) {
+  std::vector<const char*> marks;
+  r.skip_tokens(n, kSpan, marks);
+  for (size_t k = 0; k < marks.size(); ++k) {
+    Span s = proto;
+    s.start = marks[k];
+    s.first = (int64_t)k * kSpan;
+    s.n = std::min<int64_t>(kSpan, n - s.first);
+    spans.push_back(s);
+  }
+}
 
 }  // namespace
 
@@ -75,13 +224,27 @@ int gmsh_type_for(int dim, int order) {
 }
 
 MshFile read_msh(const std::string& path) {
-  std::ifstream in(path);
-  if (!in.is_open()) fail(path, "cannot open file");
+  // the whole file in memory, NUL-terminated
+  std::string buf;
+  {
+    FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) fail(path, "cannot open file");
+    std::fseek(fp, 0, SEEK_END);
+    const long sz = std::ftell(fp);
+    std::fseek(fp, 0, SEEK_SET);
+    buf.resize(sz > 0 ? (size_t)sz : 0);
+    const size_t got = sz > 0 ? std::fread(&buf[0], 1, (size_t)sz, fp) : 0;
+    std::fclose(fp);
+    if (got != buf.size()) fail(path, "read error");
+  }
   MshFile f;
-  Reader r{in, path};
-  std::string tok;
+  Reader r{buf.data(), buf.data() + buf.size(), path};
+  std::vector<Span> spans;
+  // element blocks are filled in place by the parallel pass: keep their storage stable
+  std::deque<ElementBlock> blocks;
   bool have_nodes = false, have_elems = false;
-  while (in >> tok) {
+  while (!r.at_end()) {
+    const std::string tok = r.token();
     if (tok == "$MeshFormat") {
       f.version = r.get<double>();
       int ftype = r.get<int>();
@@ -91,10 +254,10 @@ MshFile read_msh(const std::string& path) {
       r.expect("$EndMeshFormat");
     } else if (tok == "$PhysicalNames") {
       int n = r.get<int>();
-      std::string line;
-      std::getline(in, line);
+      r.line();
       for (int i = 0; i < n; ++i) {
-        if (!std::getline(in, line)) fail(path, "truncated $PhysicalNames");
+        if (r.at_end()) fail(path, "truncated $PhysicalNames");
+        const std::string line = r.line();
         std::istringstream ls(line);
         PhysicalGroup g;
         ls >> g.dim >> g.tag;
@@ -132,31 +295,26 @@ MshFile read_msh(const std::string& path) {
         r.get<int64_t>();
         r.get<int64_t>();
       }
-      f.node_tags.reserve(nnodes);
-      f.node_xyz.reserve(3 * nnodes);
+      if (nnodes < 0) fail(path, "node count mismatch");
+      f.node_tags.assign(nnodes, 0);
+      f.node_xyz.assign(3 * nnodes, 0.0);
+      int64_t base = 0;
       for (int64_t b = 0; b < nblocks; ++b) {
-        int a = r.get<int>(), c = r.get<int>();
-        (void)a;
-        (void)c;
+        r.get<int>();
+        r.get<int>();
         int parametric = r.get<int>();
         int64_t n = r.get<int64_t>();
+        if (n < 0 || base + n > nnodes) fail(path, "node count mismatch");
+        if (parametric && n > 0) fail(path, "parametric node coordinates are not supported");
         if (f.version >= 4.1) {
-          size_t base = f.node_tags.size();
-          for (int64_t i = 0; i < n; ++i) f.node_tags.push_back(r.get<int64_t>());
-          for (int64_t i = 0; i < n; ++i) {
-            for (int k = 0; k < 3; ++k) f.node_xyz.push_back(r.get<double>());
-            if (parametric) fail(path, "parametric node coordinates are not supported");
-          }
-          (void)base;
+          add_spans(r, spans, Span{nullptr, 0, 0, 0, base, 0, nullptr}, n);
+          add_spans(r, spans, Span{nullptr, 0, 0, 1, base, 0, nullptr}, 3 * n);
         } else {
-          for (int64_t i = 0; i < n; ++i) {
-            f.node_tags.push_back(r.get<int64_t>());
-            for (int k = 0; k < 3; ++k) f.node_xyz.push_back(r.get<double>());
-            if (parametric) fail(path, "parametric node coordinates are not supported");
-          }
+          add_spans(r, spans, Span{nullptr, 0, 0, 2, base, 0, nullptr}, 4 * n);
         }
+        base += n;
       }
-      if ((int64_t)f.node_tags.size() != nnodes) fail(path, "node count mismatch");
+      if (base != nnodes) fail(path, "node count mismatch");
       r.expect("$EndNodes");
     } else if (tok == "$Elements") {
       have_elems = true;
@@ -167,7 +325,8 @@ MshFile read_msh(const std::string& path) {
         r.get<int64_t>();
       }
       for (int64_t b = 0; b < nblocks; ++b) {
-        ElementBlock blk;
+        blocks.emplace_back();
+        ElementBlock& blk = blocks.back();
         int a = r.get<int>(), c = r.get<int>();
         if (f.version >= 4.1) {
           blk.dim = a;
@@ -180,13 +339,11 @@ MshFile read_msh(const std::string& path) {
         int64_t n = r.get<int64_t>();
         blk.nodes_per_elem = gmsh_type_nodes(blk.type);
         if (blk.nodes_per_elem == 0) fail(path, "unsupported element type " + std::to_string(blk.type));
+        if (n < 0) fail(path, "bad element count");
         blk.tags.resize(n);
         blk.nodes.resize(n * blk.nodes_per_elem);
-        for (int64_t i = 0; i < n; ++i) {
-          blk.tags[i] = r.get<int64_t>();
-          for (int k = 0; k < blk.nodes_per_elem; ++k) blk.nodes[i * blk.nodes_per_elem + k] = r.get<int64_t>();
-        }
-        f.blocks.push_back(std::move(blk));
+        const int per = 1 + blk.nodes_per_elem;
+        add_spans(r, spans, Span{nullptr, 0, 0, 3, 0, per, &blk}, n * per);
       }
       r.expect("$EndElements");
     } else if (!tok.empty() && tok[0] == '$' && tok.rfind("$End", 0) != 0) {
@@ -194,12 +351,14 @@ MshFile read_msh(const std::string& path) {
     }
   }
   if (!have_nodes || !have_elems) fail(path, "missing $Nodes or $Elements");
+  parse_spans(spans, f, path, buf.data() + buf.size());
+  for (auto& b : blocks) f.blocks.push_back(std::move(b));
   if (f.model_dim == 0)
     for (const auto& b : f.blocks) f.model_dim = std::max(f.model_dim, b.dim);
   return f;
 }
 
-VolumeMesh to_volume_mesh(const MshFile& f) {
+VolumeMesh to_volume_mesh(MshFile f) {
   VolumeMesh m;
   m.dim = f.model_dim;
   if (m.dim != 2 && m.dim != 3) throw std::runtime_error("mesh dimension must be 2 or 3");
@@ -213,7 +372,7 @@ VolumeMesh to_volume_mesh(const MshFile& f) {
   m.nodes_per_elem = gmsh_type_nodes(m.type);
   if (gmsh_type_dim(m.type) != m.dim) throw std::runtime_error("element type does not match model dimension");
   m.node_tags = f.node_tags;
-  m.xyz = f.node_xyz;
+  m.xyz = std::move(f.node_xyz);
   int64_t max_tag = 0;
   for (auto t : f.node_tags) max_tag = std::max(max_tag, t);
   std::vector<int64_t> tag2idx;

@@ -63,7 +63,7 @@ struct VolumeMesh {
   std::vector<std::vector<int64_t>> bc_group_nodes; // node indices per group
 };
 
-VolumeMesh to_volume_mesh(const MshFile& f);
+VolumeMesh to_volume_mesh(MshFile f);
 VolumeMesh load_volume_mesh(const std::string& path);
 
 // Writes a 4.1 ASCII mesh: one volume entity holding all elements and one
