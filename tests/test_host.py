@@ -248,3 +248,24 @@ def test_pvd_replays_schedule(pkg, tmp_path):
     assert lines[1] == '    <DataSet timestep="0.1" part="0" file="results/result100.vtu"/>'
     times, snap = pkg.host.schedule(0.0, 1.0, 1e-3, 0.1)
     assert len(times) == 1000 and np.nonzero(snap)[0].tolist() == list(range(0, 1000, 100))
+
+
+def test_msh_parallel_parse_round_trip(pkg, tmp_path):
+    """A mesh whose node and element sections span many parallel parse tasks
+    (65,536 tokens each) reads back exactly as written; a malformed number in
+    the bulk sections is reported."""
+    m = pkg.meshgen.box(counts=(16, 16, 16), order=3, seed=5)
+    path = str(tmp_path / "big.msh")
+    pkg.host.write_mesh(path, 3, 3, m["xyz"], m["elem_nodes"], [(g[0], g[1], g[3]) for g in m["groups"]])
+    r = pkg.host.load_mesh(path)
+    assert len(m["xyz"]) * 3 > 4 * 65536
+    np.testing.assert_array_equal(r["xyz"], m["xyz"])
+    np.testing.assert_array_equal(r["elem_nodes"], m["elem_nodes"])
+    txt = open(path).read()
+    i = txt.index("$Nodes")
+    j = txt.index("\n", txt.index("\n", txt.index("\n", i) + 1) + 1)  # past the section and first block headers
+    bad = txt[:j + 1] + "x" + txt[j + 1:]
+    p2 = str(tmp_path / "bad.msh")
+    open(p2, "w").write(bad)
+    with pytest.raises(RuntimeError, match="malformed"):
+        pkg.host.load_mesh(p2)
