@@ -228,18 +228,22 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   }
   if (c->variant >= 0) {
     if constexpr (sizeof(T) == 4)
-      return c->dim == 2 ? dgk::launch_stage2_f32_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
-                         : dgk::launch_stage2_f32_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
+      return c->dim == 1   ? dgk::launch_stage2_f32_1d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+             : c->dim == 2 ? dgk::launch_stage2_f32_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+                           : dgk::launch_stage2_f32_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
     else
-      return c->dim == 2 ? dgk::launch_stage2_f64_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
-                         : dgk::launch_stage2_f64_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
+      return c->dim == 1   ? dgk::launch_stage2_f64_1d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+             : c->dim == 2 ? dgk::launch_stage2_f64_2d(c->order, c->variant, a, c->grid2, c->d_err, c->stream)
+                           : dgk::launch_stage2_f64_3d(c->order, c->variant, a, c->grid2, c->d_err, c->stream);
   }
   if constexpr (sizeof(T) == 4)
-    return c->dim == 2 ? dgk::launch_stage_f32_2d(c->order, a, c->grid, c->stream)
-                       : dgk::launch_stage_f32_3d(c->order, a, c->grid, c->stream);
+    return c->dim == 1   ? dgk::launch_stage_f32_1d(c->order, a, c->grid, c->stream)
+           : c->dim == 2 ? dgk::launch_stage_f32_2d(c->order, a, c->grid, c->stream)
+                         : dgk::launch_stage_f32_3d(c->order, a, c->grid, c->stream);
   else
-    return c->dim == 2 ? dgk::launch_stage_f64_2d(c->order, a, c->grid, c->stream)
-                       : dgk::launch_stage_f64_3d(c->order, a, c->grid, c->stream);
+    return c->dim == 1   ? dgk::launch_stage_f64_1d(c->order, a, c->grid, c->stream)
+           : c->dim == 2 ? dgk::launch_stage_f64_2d(c->order, a, c->grid, c->stream)
+                         : dgk::launch_stage_f64_3d(c->order, a, c->grid, c->stream);
 }
 
 cudaError_t launch_stage(dg_ctx* c, int stage, const void* y_in, void* y_out, void* k_out, double dt) {
@@ -409,8 +413,13 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
   if (dgk::is_tc_variant(v))
     return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order, dgk::tc_npart(v))
                               : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
-  if (c->prec == DG_FP32) return c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v) : dgk::stage2_info_f32_3d(c->order, v);
-  return c->dim == 2 ? dgk::stage2_info_f64_2d(c->order, v) : dgk::stage2_info_f64_3d(c->order, v);
+  if (c->prec == DG_FP32)
+    return c->dim == 1   ? dgk::stage2_info_f32_1d(c->order, v)
+           : c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v)
+                         : dgk::stage2_info_f32_3d(c->order, v);
+  return c->dim == 1   ? dgk::stage2_info_f64_1d(c->order, v)
+         : c->dim == 2 ? dgk::stage2_info_f64_2d(c->order, v)
+                       : dgk::stage2_info_f64_3d(c->order, v);
 }
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
@@ -652,7 +661,11 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     return code;
   };
   if (!mesh || !phys || !mesh->xyz || !mesh->elem_nodes) return bad(DG_ERR_ARG, "null mesh or physics");
-  if (mesh->dim != 2 && mesh->dim != 3) return bad(DG_ERR_ARG, "dim must be 2 or 3");
+  if (mesh->dim < 1 || mesh->dim > 3) return bad(DG_ERR_ARG, "dim must be 1, 2 or 3");
+  if (mesh->dim == 1)
+    for (int64_t k = 0; k < mesh->n_nodes; ++k)
+      if (mesh->xyz[3 * k + 1] != 0.0 || mesh->xyz[3 * k + 2] != 0.0)
+        return bad(DG_ERR_MESH, "1-D meshes must lie on the x axis (y = z = 0)");
   if (mesh->order < 1 || mesh->order > 4) return bad(DG_ERR_ARG, "order must be 1..4");
   if (precision != DG_FP64 && precision != DG_FP32) return bad(DG_ERR_ARG, "precision must be DG_FP64 or DG_FP32");
   if (mesh->n_elems <= 0 || mesh->n_nodes <= 0) return bad(DG_ERR_ARG, "empty mesh");
@@ -701,7 +714,9 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
     double J[3][3] = {{0}}, Gi[3][3] = {{0}};
     for (int k = 0; k < D; ++k)
       for (int d = 0; d < D; ++d) J[d][k] = mesh->xyz[3 * en[k + 1] + d] - x0[d];
-    if (D == 2) {
+    if (D == 1) {
+      Gi[0][0] = 1.0 / J[0][0];
+    } else if (D == 2) {
       double dt = J[0][0] * J[1][1] - J[0][1] * J[1][0];
       Gi[0][0] = J[1][1] / dt, Gi[0][1] = -J[0][1] / dt, Gi[1][0] = -J[1][0] / dt, Gi[1][1] = J[0][0] / dt;
     } else {
@@ -757,9 +772,13 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
   // blocks per SM for the persistent stage kernel
   int bps = 1;
   if (c->prec == DG_FP32)
-    bps = c->dim == 2 ? dgk::blocks_per_sm_f32_2d(c->order) : dgk::blocks_per_sm_f32_3d(c->order);
+    bps = c->dim == 1   ? dgk::blocks_per_sm_f32_1d(c->order)
+          : c->dim == 2 ? dgk::blocks_per_sm_f32_2d(c->order)
+                        : dgk::blocks_per_sm_f32_3d(c->order);
   else
-    bps = c->dim == 2 ? dgk::blocks_per_sm_f64_2d(c->order) : dgk::blocks_per_sm_f64_3d(c->order);
+    bps = c->dim == 1   ? dgk::blocks_per_sm_f64_1d(c->order)
+          : c->dim == 2 ? dgk::blocks_per_sm_f64_2d(c->order)
+                        : dgk::blocks_per_sm_f64_3d(c->order);
   c->grid = (int)std::min<int64_t>(c->ntiles, (int64_t)bps * c->num_sms);
   const size_t ts = c->tsize;
   const int64_t nstate = (int64_t)c->nv * c->Epad * c->np;

@@ -472,6 +472,10 @@ int setup_curved(dg_ctx* c, const double* xyz, const int64_t* en, const int* per
     c->ncurved = (int64_t)celem.size();
     if (c->ncurved == 0) return DG_OK;
     if (c->order < 2) throw std::runtime_error("curved elements need order >= 2");
+    if (c->dim == 1) {
+      c->err = "mesh setup failed: 1-D elements must have equispaced nodes;";
+      return DG_ERR_MESH;
+    }
     const int D = c->dim, np = c->np, nf = c->nf, nfp = c->nfp, NV = c->nv;
     const int64_t nc = c->ncurved;
     const dgref::CurvedTables tb = dgref::build_curved(c->re);

@@ -29,11 +29,11 @@ constexpr int kCodeBoundary = 1 << 6;    // boundary face; nbr slot holds the bo
 // Compile-time shape of a (dim, order) pair.
 template <int D, int P>
 struct Shape {
-  static constexpr int NP = D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6;
+  static constexpr int NP = D == 1 ? P + 1 : D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6;
   static constexpr int NF = D + 1;
-  static constexpr int NFP = D == 2 ? P + 1 : (P + 1) * (P + 2) / 2;
+  static constexpr int NFP = D == 1 ? 1 : D == 2 ? P + 1 : (P + 1) * (P + 2) / 2;
   static constexpr int NV = D + 1;
-  static constexpr int NPERM = D == 2 ? 2 : 6;
+  static constexpr int NPERM = D == 1 ? 1 : D == 2 ? 2 : 6;
   // threads per element: each owns a chunk of NC output nodes
   static constexpr int NCMAX = D == 2 ? 6 : 5;
   static constexpr int NSPLIT = (NP + NCMAX - 1) / NCMAX;
@@ -175,6 +175,15 @@ Stage2Info stage2_info_f32_2d(int order, int variant);
 Stage2Info stage2_info_f32_3d(int order, int variant);
 Stage2Info stage2_info_f64_2d(int order, int variant);
 Stage2Info stage2_info_f64_3d(int order, int variant);
+// 1-D (line elements, stage_1d.cu): the same families for both precisions.
+cudaError_t launch_stage_f32_1d(int order, const StageArgs<float>& a, int grid, cudaStream_t s);
+cudaError_t launch_stage_f64_1d(int order, const StageArgs<double>& a, int grid, cudaStream_t s);
+int blocks_per_sm_f32_1d(int order);
+int blocks_per_sm_f64_1d(int order);
+cudaError_t launch_stage2_f32_1d(int order, int variant, const StageArgs<float>& a, int grid, int* err, cudaStream_t s);
+cudaError_t launch_stage2_f64_1d(int order, int variant, const StageArgs<double>& a, int grid, int* err, cudaStream_t s);
+Stage2Info stage2_info_f32_1d(int order, int variant);
+Stage2Info stage2_info_f64_1d(int order, int variant);
 // Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant ids
 // kTcVariant (2 threads per tile row, 256 per block) and kTcVariant + 1
 // (4 threads per row, 512 per block) of the context's kernel selection.
@@ -220,6 +229,7 @@ inline ShapeInfo shape_info(int dim, int order) {
     return ShapeInfo{Shape<D, P>::NP,     Shape<D, P>::NF,     Shape<D, P>::NFP,           Shape<D, P>::NV, \
                      Shape<D, P>::NPERM,  Shape<D, P>::ET,     Shape<D, P>::NT,            ShapeT<D, P, float>::RECF, \
                      ShapeT<D, P, double>::RECF, Shape<D, P>::RECI};
+  DGK_SHAPE(1, 1) DGK_SHAPE(1, 2) DGK_SHAPE(1, 3) DGK_SHAPE(1, 4)
   DGK_SHAPE(2, 1) DGK_SHAPE(2, 2) DGK_SHAPE(2, 3) DGK_SHAPE(2, 4)
   DGK_SHAPE(3, 1) DGK_SHAPE(3, 2) DGK_SHAPE(3, 3) DGK_SHAPE(3, 4)
 #undef DGK_SHAPE

@@ -361,7 +361,7 @@ MshFile read_msh(const std::string& path) {
 VolumeMesh to_volume_mesh(MshFile f) {
   VolumeMesh m;
   m.dim = f.model_dim;
-  if (m.dim != 2 && m.dim != 3) throw std::runtime_error("mesh dimension must be 2 or 3");
+  if (m.dim < 1 || m.dim > 3) throw std::runtime_error("mesh dimension must be 1, 2 or 3");
   for (const auto& b : f.blocks)
     if (b.dim == m.dim) {
       m.type = b.type;

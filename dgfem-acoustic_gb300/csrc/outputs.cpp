@@ -219,7 +219,7 @@ void write_vtu(const std::string& path, int dim, const std::vector<int64_t>& nod
     for (int d = 0; d < 3; ++d) pts[3 * (node_tags[i] - 1) + d] = xyz[3 * i + d];
   int nc = dim + 1;
   std::vector<int64_t> conn(E * nc), offs(E);
-  std::vector<uint8_t> types(E, dim == 3 ? 10 : 5);
+  std::vector<uint8_t> types(E, dim == 3 ? 10 : dim == 2 ? 5 : 3);  // VTK_TETRA, VTK_TRIANGLE, VTK_LINE
   for (int64_t e = 0; e < E; ++e) {
     for (int k = 0; k < nc; ++k) conn[e * nc + k] = node_tags[elem_nodes[e * nodes_per_elem + k]] - 1;
     offs[e] = (e + 1) * nc;

@@ -137,6 +137,7 @@ const int kTetFaces[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {3, 1, 2}};
 
 int lattice_index(const RefElement& re, const int* ijk) {
   int p = re.p;
+  if (re.dim == 1) return (ijk[0] >= 0 && ijk[0] <= p) ? ijk[0] : -1;
   if (re.dim == 2) {
     int i = ijk[0], j = ijk[1];
     if (i < 0 || j < 0 || i + j > p) return -1;
@@ -198,18 +199,20 @@ int recipe_normal_sign(int dim, int p) {
 }
 
 RefElement build(int dim, int p) {
-  if (dim != 2 && dim != 3) throw std::runtime_error("dim must be 2 or 3");
+  if (dim < 1 || dim > 3) throw std::runtime_error("dim must be 1, 2 or 3");
   if (p < 1 || p > kMaxP) throw std::runtime_error("order must be 1..4");
   RefElement re;
   re.dim = dim, re.p = p;
-  re.np = dim == 2 ? (p + 1) * (p + 2) / 2 : (p + 1) * (p + 2) * (p + 3) / 6;
+  re.np = dim == 1 ? p + 1 : dim == 2 ? (p + 1) * (p + 2) / 2 : (p + 1) * (p + 2) * (p + 3) / 6;
   re.nf = dim + 1;
-  re.nfp = dim == 2 ? p + 1 : (p + 1) * (p + 2) / 2;
-  re.ref_measure = dim == 2 ? 0.5 : 1.0 / 6.0;
-  re.face_ref_measure = dim == 2 ? 1.0 : 0.5;
+  re.nfp = dim == 1 ? 1 : dim == 2 ? p + 1 : (p + 1) * (p + 2) / 2;
+  re.ref_measure = dim == 1 ? 1.0 : dim == 2 ? 0.5 : 1.0 / 6.0;
+  re.face_ref_measure = dim == 3 ? 0.5 : 1.0;  // a point face has measure 1
   // lattice in internal order
   re.lattice.clear();
-  if (dim == 2) {
+  if (dim == 1) {
+    for (int i = 0; i <= p; ++i) re.lattice.push_back(i);
+  } else if (dim == 2) {
     for (int j = 0; j <= p; ++j)
       for (int i = 0; i <= p - j; ++i) re.lattice.push_back(i), re.lattice.push_back(j);
   } else {
@@ -228,10 +231,13 @@ RefElement build(int dim, int p) {
     return re.lattice[n * D + v - 1];
   };
   for (int f = 0; f < nf; ++f)
-    for (int k = 0; k < D; ++k) re.face_corners[f][k] = D == 2 ? kTriEdges[f][k] : kTetFaces[f][k];
+    // lines: local face f is the end point at vertex f
+    for (int k = 0; k < D; ++k) re.face_corners[f][k] = D == 1 ? f : D == 2 ? kTriEdges[f][k] : kTetFaces[f][k];
   // face lattice: (a1, a2) with a0 = p - a1 - a2, a2 outer
   std::vector<int> flat;  // nfp * 3 face barycentrics (a0,a1,a2)
-  if (D == 2) {
+  if (D == 1) {
+    flat.push_back(p), flat.push_back(0), flat.push_back(0);
+  } else if (D == 2) {
     for (int a1 = 0; a1 <= p; ++a1) flat.push_back(p - a1), flat.push_back(a1), flat.push_back(0);
   } else {
     for (int a2 = 0; a2 <= p; ++a2)
@@ -259,11 +265,11 @@ RefElement build(int dim, int p) {
     }
   }
   // permutations of the face corners: our corner k sits at neighbour position perm[k]
-  re.nperm = D == 2 ? 2 : 6;
+  re.nperm = D == 1 ? 1 : D == 2 ? 2 : 6;
   const int perms3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
   const int perms2[2][3] = {{0, 1, 2}, {1, 0, 2}};
   for (int q = 0; q < re.nperm; ++q)
-    for (int k = 0; k < 3; ++k) re.perm_table[q][k] = D == 2 ? perms2[q][k] : perms3[q][k];
+    for (int k = 0; k < 3; ++k) re.perm_table[q][k] = D == 3 ? perms3[q][k] : perms2[q][k];
   re.nbrnode.assign(nf * re.nperm * nfp, -1);
   for (int lf = 0; lf < nf; ++lf)
     for (int q = 0; q < re.nperm; ++q)
@@ -303,17 +309,22 @@ RefElement build(int dim, int p) {
         re.Dt[(r * np + i) * np + j] = s;
       }
   }
-  // face mass on the face lattice (face coordinates a1/p [, a2/p])
-  std::vector<double> fnodes(nfp * (D - 1));
-  for (int m = 0; m < nfp; ++m)
-    for (int d = 0; d < D - 1; ++d) fnodes[m * (D - 1) + d] = (double)flat[m * 3 + 1 + d] / p;
-  auto fex = monomials(D - 1, p);
-  auto FC = lagrange_coeffs(D - 1, p, fnodes, fex);
-  re.Mf = gram(nfp, FC, FC, [&](int k, int l) {
-    int e[3];
-    for (int d = 0; d < D - 1; ++d) e[d] = fex[k * (D - 1) + d] + fex[l * (D - 1) + d];
-    return mono_int(D - 1, e);
-  });
+  // face mass on the face lattice (face coordinates a1/p [, a2/p]); a point
+  // face (lines) has the 1 x 1 mass 1
+  if (D == 1) {
+    re.Mf.assign(1, 1.0);
+  } else {
+    std::vector<double> fnodes(nfp * (D - 1));
+    for (int m = 0; m < nfp; ++m)
+      for (int d = 0; d < D - 1; ++d) fnodes[m * (D - 1) + d] = (double)flat[m * 3 + 1 + d] / p;
+    auto fex = monomials(D - 1, p);
+    auto FC = lagrange_coeffs(D - 1, p, fnodes, fex);
+    re.Mf = gram(nfp, FC, FC, [&](int k, int l) {
+      int e[3];
+      for (int d = 0; d < D - 1; ++d) e[d] = fex[k * (D - 1) + d] + fex[l * (D - 1) + d];
+      return mono_int(D - 1, e);
+    });
+  }
   // LIFT = Minv E_f Mf, columns grouped by face
   re.LIFT.assign(np * nf * nfp, 0.0);
   for (int f = 0; f < nf; ++f)

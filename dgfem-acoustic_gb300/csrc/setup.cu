@@ -70,7 +70,10 @@ __global__ void k_elem_geom(SetupDev s, double* det, double* G, int* curved, int
   }
   double Gi[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   double dt;
-  if (D == 2) {
+  if (D == 1) {
+    dt = J[0][0];
+    Gi[0][0] = 1.0 / dt;
+  } else if (D == 2) {
     dt = J[0][0] * J[1][1] - J[0][1] * J[1][0];
     Gi[0][0] = J[1][1] / dt, Gi[0][1] = -J[0][1] / dt;
     Gi[1][0] = -J[1][0] / dt, Gi[1][1] = J[0][0] / dt;
@@ -109,7 +112,9 @@ __global__ void k_elem_geom(SetupDev s, double* det, double* G, int* curved, int
     }
     // internal index of the lattice point (same enumeration as dgref::lattice_index)
     int p = s.order, idx = -1;
-    if (D == 2) {
+    if (D == 1) {
+      if (lat[0] >= 0 && lat[0] <= p) idx = lat[0];
+    } else if (D == 2) {
       if (lat[0] >= 0 && lat[1] >= 0 && lat[0] + lat[1] <= p) {
         idx = 0;
         for (int jj = 0; jj < lat[1]; ++jj) idx += p - jj + 1;
@@ -137,6 +142,7 @@ __global__ void k_mark_corners(SetupDev s, int* mark) {
 
 __device__ __forceinline__ unsigned long long face_key(const SetupDev& s, const int* vid, int64_t e, int lf) {
   const int64_t* en = s.en + e * s.np;
+  if (s.dim == 1) return (unsigned long long)vid[en[s.face_corners[lf][0]]];  // a point face: its vertex
   unsigned long long a = vid[en[s.face_corners[lf][0]]], b = vid[en[s.face_corners[lf][1]]];
   unsigned long long c = s.dim == 3 ? (unsigned long long)vid[en[s.face_corners[lf][2]]] : 0ull;
   // sort (a, b[, c])
@@ -222,10 +228,15 @@ __global__ void k_face_geom(SetupDev s, const double* det, const int64_t* partne
   const int64_t* en = s.en + e * s.np;
   int64_t cn[3] = {en[s.face_corners[lf][0]], en[s.face_corners[lf][1]], D == 3 ? en[s.face_corners[lf][2]] : -1};
   const double* x0 = X(s, cn[0]);
-  const double* x1 = X(s, cn[1]);
+  const double* x1 = D >= 2 ? X(s, cn[1]) : x0;
   double sg = det[e] > 0 ? 1.0 : -1.0;
   double n[3] = {0, 0, 0}, Jf;
-  if (D == 2) {
+  if (D == 1) {
+    // point face (Mesh.cpp:320-325 and the outward flip of :536-568): the
+    // element's outward direction along x; Gmsh's point Jacobian is 1
+    Jf = 1.0;
+    n[0] = lf == 1 ? sg : -sg;
+  } else if (D == 2) {
     double tx = x1[0] - x0[0], ty = x1[1] - x0[1];
     Jf = sqrt(tx * tx + ty * ty);
     n[0] = sg * ty / Jf, n[1] = -sg * tx / Jf;
@@ -259,6 +270,12 @@ __global__ void k_face_geom(SetupDev s, const double* det, const int64_t* partne
     }
     int64_t up = e < e2 ? e : e2;
     int sf = s.fc_kappa * (det[up] > 0 ? 1 : -1);
+    if (D == 1) {
+      // s_f = orientation of the face seen from up (fc = 1): +1 at its
+      // right end point, -1 at its left one
+      const int lfu = up == e ? lf : lf2;
+      sf = (lfu == 1 ? 1 : -1) * (det[up] > 0 ? 1 : -1);
+    }
     nbr = (int)e2;
     code = lf2 | (q << dgk::kCodePermShift) | (sf < 0 ? dgk::kCodeNegPenalty : 0);
   } else {
@@ -285,7 +302,9 @@ __global__ void k_face_geom(SetupDev s, const double* det, const int64_t* partne
       }
     } else {
       double t[3] = {0, 0, 0}, sb[3] = {0, 0, 0};
-      if (D == 2) {
+      if (D == 1) {
+        // point faces carry no tangent frame (Mesh.cpp:320-325)
+      } else if (D == 2) {
         t[0] = -n[1], t[1] = n[0];
         normalize3(t);
       } else {

@@ -133,13 +133,15 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
         for (int q = 0; q < NV; ++q) up[q] = ldg(a.y_in + q * stride + (int64_t)nbr * NP + nn);
         const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
         const T* ev0 = sGF + e * RECF + S::PHYS_OFF;
-        T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
-        if (D == 3) vn0 += ev0[2] * n[2];
+        T vn0 = ev0[0] * n[0];
+        #pragma unroll
+        for (int d = 1; d < D; ++d) vn0 += ev0[d] * n[d];
         T avg[NV], dif[NV];
 #pragma unroll
         for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
-        T nv = n[0] * avg[1] + n[1] * avg[2];
-        if (D == 3) nv += n[2] * avg[3];
+        T nv = n[0] * avg[1];
+        #pragma unroll
+        for (int d = 1; d < D; ++d) nv += n[d] * avg[1 + d];
         h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
 #pragma unroll
         for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
@@ -183,8 +185,9 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
       T gv0[D];
 #pragma unroll
       for (int r = 0; r < D; ++r) {
-        gv0[r] = G[r * D + 0] * ev0[0] + G[r * D + 1] * ev0[1];
-        if (D == 3) gv0[r] += G[r * D + 2] * ev0[2];
+        gv0[r] = G[r * D + 0] * ev0[0];
+        #pragma unroll
+        for (int d = 1; d < D; ++d) gv0[r] += G[r * D + d] * ev0[d];
       }
 #pragma unroll
       for (int ii = 0; ii < NC; ++ii) {

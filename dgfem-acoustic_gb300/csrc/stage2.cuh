@@ -214,13 +214,15 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
       }
       const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
       const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
-      T vn0 = ev0[0] * n[0] + ev0[1] * n[1];
-      if (D == 3) vn0 += ev0[2] * n[2];
+      T vn0 = ev0[0] * n[0];
+      #pragma unroll
+      for (int d = 1; d < D; ++d) vn0 += ev0[d] * n[d];
       T avg[NV], dif[NV];
 #pragma unroll
       for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
-      T nv = n[0] * avg[1] + n[1] * avg[2];
-      if (D == 3) nv += n[2] * avg[3];
+      T nv = n[0] * avg[1];
+      #pragma unroll
+      for (int d = 1; d < D; ++d) nv += n[d] * avg[1 + d];
       h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
 #pragma unroll
       for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
@@ -329,8 +331,9 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
     T gv0[D];
 #pragma unroll
     for (int r = 0; r < D; ++r) {
-      gv0[r] = g[r][0] * ev0[0] + g[r][1] * ev0[1];
-      if (D == 3) gv0[r] += g[r][2] * ev0[2];
+      gv0[r] = g[r][0] * ev0[0];
+      #pragma unroll
+      for (int d = 1; d < D; ++d) gv0[r] += g[r][d] * ev0[d];
     }
 #pragma unroll
     for (int ii = 0; ii < NC; ++ii) {

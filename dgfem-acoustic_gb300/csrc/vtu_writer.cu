@@ -263,7 +263,7 @@ int dg_vtu_writer_create(dg_ctx* c, int64_t n_points, const double* points, cons
     }
   // mesh part, encoded once
   std::vector<int64_t> offs(c->E);
-  std::vector<uint8_t> types(c->E, c->dim == 3 ? 10 : 5);  // VTK_TETRA, VTK_TRIANGLE
+  std::vector<uint8_t> types(c->E, c->dim == 3 ? 10 : c->dim == 2 ? 5 : 3);  // VTK_TETRA, VTK_TRIANGLE, VTK_LINE
   for (int64_t e = 0; e < c->E; ++e) offs[e] = (e + 1) * nc;
   try {
     const std::string a = encode(points, (uint64_t)n_points * 24, w->compress, w->level, w->threads);

@@ -265,3 +265,30 @@ def warp(mesh, amp, center=None, radius=None):
             Y[:, d] += f / np.sqrt(dim)
     m["xyz"] = Y
     return m
+
+
+def line(n=100, x0=-5.0, x1=5.0, order=1, jitter=0.0, seed=3, side_names=("left", "right")):
+    """1-D mesh of n line elements on [x0, x1] along the x axis, nodes in
+    Gmsh's line order (the two end points, then the interior nodes from the
+    first to the second). The two end points are the boundary groups
+    (tags 1, 2)."""
+    rng = np.random.default_rng(seed)
+    h = (x1 - x0) / n
+    xv = x0 + h * np.arange(n + 1)
+    if jitter > 0 and n > 1:
+        xv[1:-1] += rng.uniform(-jitter * h, jitter * h, size=n - 1)
+    nv = n + 1
+    xyz = [np.stack([xv, np.zeros(nv), np.zeros(nv)], axis=1)]
+    elems = np.zeros((n, order + 1), dtype=np.int64)
+    elems[:, 0] = np.arange(n)
+    elems[:, 1] = np.arange(1, n + 1)
+    nxt = nv
+    for k in range(1, order):
+        xk = xv[:-1] + (xv[1:] - xv[:-1]) * k / order
+        xyz.append(np.stack([xk, np.zeros(n), np.zeros(n)], axis=1))
+        elems[:, 1 + k] = nxt + np.arange(n)
+        nxt += n
+    xyz = np.concatenate(xyz)
+    groups = [(1, side_names[0], np.array([0], np.int64), np.array([[0]], np.int64)),
+              (2, side_names[1], np.array([n], np.int64), np.array([[n]], np.int64))]
+    return dict(dim=1, order=order, xyz=xyz, elem_nodes=elems, groups=groups)

@@ -161,10 +161,19 @@ void gauss_jacobi(int n, double a, std::vector<double>& x, std::vector<double>& 
   }
 }
 
+// Gauss-Legendre on the oracle's [0, 1] reference segment (line elements).
+Rule line01_rule(int n);
+
 Rule gauss_line(int n) {
   Rule r;
   r.n = n, r.dim = 1;
   gauss_jacobi(n, 0.0, r.x, r.w);
+  return r;
+}
+
+Rule line01_rule(int n) {
+  Rule r = gauss_line(n);
+  for (int g = 0; g < n; ++g) r.x[g] = 0.5 * (r.x[g] + 1.0), r.w[g] *= 0.5;
   return r;
 }
 
@@ -421,8 +430,8 @@ void RefMesh::setup(const refcpu_input* input) {
   m_elNumNodes = in->nodes_per_elem;
   m_elNum = (int)in->n_elems;
   const int D = m_elDim, P = m_elOrder, Np = m_elNumNodes;
-  if (D != 2 && D != 3) throw std::runtime_error("dim must be 2 or 3");
-  int expectNp = D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6;
+  if (D < 1 || D > 3) throw std::runtime_error("dim must be 1, 2 or 3");
+  int expectNp = D == 1 ? P + 1 : D == 2 ? (P + 1) * (P + 2) / 2 : (P + 1) * (P + 2) * (P + 3) / 6;
   if (Np != expectNp) throw std::runtime_error("nodes_per_elem does not match order");
   const int nc = D + 1;
 
@@ -461,7 +470,9 @@ void RefMesh::setup(const refcpu_input* input) {
   elBasis.build(D, P, refNodes);
 
   // --- volume quadrature, basis at points, Jacobians (Mesh.cpp:40-137) ---
-  Rule vr = D == 2 ? tri_rule(2 * P) : tet_rule(2 * P);
+  // lines: Gauss-Legendre with P + 1 points (degree 2P + 1), on the
+  // oracle's [0, 1] reference segment
+  Rule vr = D == 1 ? line01_rule(P + 1) : D == 2 ? tri_rule(2 * P) : tet_rule(2 * P);
   m_elNumIntPts = vr.n;
   const int Ng = vr.n;
   m_elWeight = vr.w;
@@ -480,9 +491,12 @@ void RefMesh::setup(const refcpu_input* input) {
       for (int n = 0; n < Np; ++n)
         for (int x = 0; x < D; ++x)
           for (int u = 0; u < D; ++u) J[x * D + u] += X(en[n])[x] * ugrad[(g * Np + n) * D + u];
-      double det = D == 2 ? J[0] * J[3] - J[1] * J[2]
-                          : J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
-                                J[2] * (J[3] * J[7] - J[4] * J[6]);
+      // Gmsh's determinant of a line element in 3-D space is the length of
+      // its tangent (positive); simplices keep the signed determinant
+      double det = D == 1   ? std::fabs(J[0])
+                   : D == 2 ? J[0] * J[3] - J[1] * J[2]
+                            : J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                                  J[2] * (J[3] * J[7] - J[4] * J[6]);
       m_elJacobianDets[el * Ng + g] = det;
       // J^T grad_x = grad_u (src/Mesh.cpp:132-133)
       std::vector<double> JT(D * D);
@@ -499,7 +513,7 @@ void RefMesh::setup(const refcpu_input* input) {
 
   // --- faces of all elements (Mesh.cpp:165-183) ---
   m_fDim = D - 1;
-  m_fNumNodes = m_fDim == 1 ? 1 + P : (P + 1) * (P + 2) / 2;
+  m_fNumNodes = m_fDim == 0 ? 1 : m_fDim == 1 ? 1 + P : (P + 1) * (P + 2) / 2;
   m_fNumPerEl = D + 1;
   const int Nf = m_fNumPerEl, Nfp = m_fNumNodes;
   // element-local face node lists: corners in face order, then the rest
@@ -507,7 +521,8 @@ void RefMesh::setup(const refcpu_input* input) {
   std::vector<double> faceRefNodes(Nf * Nfp * (D - 1));
   for (int lf = 0; lf < Nf; ++lf) {
     int corners[3];
-    for (int k = 0; k < D; ++k) corners[k] = D == 2 ? kTriEdges[lf][k] : kTetFaces[lf][k];
+    // lines: the faces are the two end points, local face lf = vertex lf
+    for (int k = 0; k < D; ++k) corners[k] = D == 1 ? lf : D == 2 ? kTriEdges[lf][k] : kTetFaces[lf][k];
     int opp = 0;
     for (int v = 0; v < nc; ++v) {
       bool in_face = false;
@@ -540,7 +555,9 @@ void RefMesh::setup(const refcpu_input* input) {
     if (cnt != Nfp) throw std::runtime_error("face node count mismatch");
     for (int m = 0; m < Nfp; ++m) {
       int n = m_locFaceNodes[lf * Nfp + m];
-      if (D == 2) {
+      if (D == 1) {
+        // point faces have no reference coordinates
+      } else if (D == 2) {
         faceRefNodes[(lf * Nfp + m)] = 2.0 * bary(n, corners[1]) / P - 1.0;
       } else {
         faceRefNodes[(lf * Nfp + m) * 2 + 0] = (double)bary(n, corners[1]) / P;
@@ -550,7 +567,7 @@ void RefMesh::setup(const refcpu_input* input) {
   }
   // All local faces share one face-node arrangement by construction; use face 0's.
   Basis fBasis;
-  fBasis.build(D - 1, P, std::vector<double>(faceRefNodes.begin(), faceRefNodes.begin() + Nfp * (D - 1)));
+  if (D > 1) fBasis.build(D - 1, P, std::vector<double>(faceRefNodes.begin(), faceRefNodes.begin() + Nfp * (D - 1)));
   for (int lf = 1; lf < Nf; ++lf)
     for (int k = 0; k < Nfp * (D - 1); ++k)
       if (std::fabs(faceRefNodes[lf * Nfp * (D - 1) + k] - faceRefNodes[k]) > 1e-12)
@@ -580,9 +597,9 @@ void RefMesh::setup(const refcpu_input* input) {
   for (int64_t el = 0; el < m_elNum; ++el) {
     const int64_t* en = &in->elem_nodes[el * Np];
     for (int lf = 0; lf < Nf; ++lf) {
-      int64_t v[3] = {en[m_locFaceNodes[lf * Nfp + 0]], en[m_locFaceNodes[lf * Nfp + 1]],
+      int64_t v[3] = {en[m_locFaceNodes[lf * Nfp + 0]], D >= 2 ? en[m_locFaceNodes[lf * Nfp + 1]] : -1,
                       D == 3 ? en[m_locFaceNodes[lf * Nfp + 2]] : -1};
-      std::sort(v, v + (D == 3 ? 3 : 2));
+      std::sort(v, v + D);
       Key k{v[0], v[1], v[2]};
       auto it = faceOf.find(k);
       int64_t f;
@@ -604,13 +621,22 @@ void RefMesh::setup(const refcpu_input* input) {
   const int64_t F = m_fNum;
 
   // --- face quadrature, basis, Jacobians, tangential gradients (Mesh.cpp:209-260) ---
-  Rule fr = D == 2 ? gauss_line(P + 1) : tri_rule(2 * P);
+  // point faces (lines): one point of weight 1, face basis 1
+  Rule fr;
+  if (D == 1)
+    fr.n = 1, fr.dim = 0, fr.w = {1.0};
+  else
+    fr = D == 2 ? gauss_line(P + 1) : tri_rule(2 * P);
   m_fNumIntPts = fr.n;
   const int Ngf = fr.n;
   m_fWeight = fr.w;
   m_fBasisFcts.resize(Ngf * Nfp);
   std::vector<double> fugrad(Ngf * Nfp * (D - 1));
   for (int g = 0; g < Ngf; ++g) {
+    if (D == 1) {
+      m_fBasisFcts[g * Nfp] = 1.0;
+      continue;
+    }
     fBasis.eval(&fr.x[g * (D - 1)], &m_fBasisFcts[g * Nfp]);
     fBasis.grad(&fr.x[g * (D - 1)], &fugrad[g * Nfp * (D - 1)]);
   }
@@ -629,7 +655,9 @@ void RefMesh::setup(const refcpu_input* input) {
       }
       for (int x = 0; x < 3; ++x) m_fIntPtCoords[(f * Ngf + g) * 3 + x] = xg[x];
       double det;
-      if (D == 2) {
+      if (D == 1) {
+        det = 1.0;  // Gmsh's Jacobian determinant of a point element
+      } else if (D == 2) {
         det = std::sqrt(dot3(T[0], T[0]));
         for (int n = 0; n < Nfp; ++n) {
           double c = fugrad[g * Nfp + n] / (det * det);
@@ -677,7 +705,12 @@ void RefMesh::setup(const refcpu_input* input) {
     }
     for (int g = 0; g < Ngf; ++g) {
       double normal[3], tangent[3], bitangent[3];
-      if (m_fDim == 1) {
+      if (m_fDim == 0) {
+        // Mesh.cpp:320-325: every point face has the normal (1, 0, 0)
+        normal[0] = 1.0, normal[1] = normal[2] = 0.0;
+        tangent[0] = tangent[1] = tangent[2] = 0.0;
+        bitangent[0] = bitangent[1] = bitangent[2] = 0.0;
+      } else if (m_fDim == 1) {
         const double plane[3] = {0, 0, -1};
         cross3(fg(f, g, 0), plane, normal);
         if (dot3(fg(f, g, 0), fg(f, 0, 0)) < 0)

@@ -1,13 +1,16 @@
-"""Regenerates the golden fixtures of the reference's 2d_hilltop case.
+"""Regenerates the golden fixtures of the reference's 2d_hilltop case and its
+1-D example mesh.
 
 Reads, from a checkout of the reference (default /root/reference):
   residuals.csv                          per-step residual trace of a reference run
   cases/2d_hilltop/2d_hilltop_fs.msh     its mesh
   cases/2d_hilltop/2d_hilltop.json       its configuration
+  doc/1d/line.msh                        the 1-D example mesh (100 lines on [-5, 5])
 and writes next to this script:
   hilltop_residuals.csv   time;res_p;res_rho;res_vx;res_vy (elapsed time dropped)
   2d_hilltop_fs.msh.gz    the mesh, gzip-compressed
   2d_hilltop.json         the configuration with the mesh path made relative
+  line_1d.msh             the 1-D mesh as is
 """
 import gzip
 import json
@@ -32,6 +35,8 @@ def main(ref="/root/reference"):
     cfg["mesh"]["File"] = "2d_hilltop_fs.msh"
     with open(os.path.join(HERE, "2d_hilltop.json"), "w") as f:
         json.dump(cfg, f, indent=1)
+    with open(os.path.join(ref, "doc/1d/line.msh"), "rb") as src, open(os.path.join(HERE, "line_1d.msh"), "wb") as dst:
+        dst.write(src.read())
 
 
 if __name__ == "__main__":

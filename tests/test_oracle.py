@@ -108,3 +108,59 @@ def test_golden_trace_discriminates(pkg, oracle):
     gold = np.genfromtxt(os.path.join(GOLDEN, "hilltop_residuals.csv"), delimiter=";", skip_header=1)
     rows = np.arange(160, 200)
     assert np.max(np.abs(r["residuals"][rows, 0] - gold[rows, 1]) / gold[rows, 1]) > 1e-2
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_line_linear_fields_give_exact_derivatives(pkg, oracle, p):
+    """1-D line elements (point faces with the reference's (1, 0, 0) normal,
+    line Jacobian |dx/du|): on interior elements dv/dt = -dp/dx / rho0 and
+    dp/dt = -rho0 c0^2 dv/dx exactly for linear fields, also on elements whose
+    end points are listed right to left; every interior face of a
+    left-to-right mesh has penalty sign +1."""
+    mg = pkg.meshgen
+    m = mg.line(n=8, order=p, jitter=0.2, seed=p)
+    mesh = dict(dim=1, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"], groups=[])
+    f = oracle.Problem(mesh, dt=1.0).faces()
+    assert np.all(f["penalty"][f["nbr"] >= 0] == 1)
+    en = m["elem_nodes"].copy()
+    en[3, 0], en[3, 1] = en[3, 1], en[3, 0]
+    if p > 1:
+        en[3, 2:] = en[3, 2:][::-1]
+    mesh["elem_nodes"] = en
+    rho0, c0 = 1.3, 2.0
+    P = oracle.Problem(mesh, rho0=rho0, c0=c0, dt=1.0)
+    x = mesh["xyz"][en.reshape(-1), 0]
+    interior = (P.faces()["nbr"] >= 0).all(axis=1)
+    u = np.zeros((4, x.size))
+    u[0] = 2.0 * x
+    u[1] = -0.5 * x
+    k = P.stage(u).reshape(4, -1, p + 1)
+    np.testing.assert_allclose(k[1][interior], -2.0 / rho0, rtol=1e-10)
+    np.testing.assert_allclose(k[0][interior], 0.5 * rho0 * c0 ** 2, rtol=1e-10)
+    assert np.all(k[2:] == 0.0)
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_line_rhs_converges(pkg, oracle, p):
+    """Smooth fields: the 1-D right-hand side approaches the exact time
+    derivative at order p under mesh refinement (interior nodes)."""
+    mg = pkg.meshgen
+    errs = []
+    for n in (16, 32):
+        m = mg.line(n=n, order=p)
+        mesh = dict(dim=1, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                    groups=mg.solver_groups(m, {"left": "Reflecting", "right": "Reflecting"}))
+        x = m["xyz"][m["elem_nodes"].reshape(-1), 0]
+        u = np.zeros((4, x.size))
+        u[0], u[1] = np.sin(x), np.cos(x)
+        k = oracle.Problem(mesh, dt=1.0, rho0=1.2, c0=3.0).stage(u)
+        inner = np.abs(x) < 3.5
+        errs.append(np.linalg.norm((k[1] + np.cos(x) / 1.2)[inner]) / np.linalg.norm(np.cos(x)[inner] / 1.2))
+    assert errs[1] < errs[0] / 2 ** (p - 0.5), errs
+
+
+def test_reference_line_mesh_loads(pkg):
+    m = pkg.host.load_mesh(os.path.join(GOLDEN, "line_1d.msh"))
+    assert m["dim"] == 1 and m["order"] == 1 and m["elem_nodes"].shape == (100, 2)
+    assert np.all(m["xyz"][:, 1:] == 0.0) and m["xyz"][:, 0].min() == -5.0 and m["xyz"][:, 0].max() == 5.0
+    assert len(m["groups"]) == 1 and sorted(m["groups"][0][2].tolist()) == [0, 1]
