@@ -81,7 +81,10 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // VW-wide vector load/store of T (VW in {1, 2, 4}; addresses VW-aligned).
 template <typename T, int VW>
 __device__ __forceinline__ void vload(T* r, const T* p) {
-  if constexpr (VW == 4 && sizeof(T) == 4) {
+  if constexpr (VW == 4 && sizeof(T) == 8) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    r[0] = a.x, r[1] = a.y, r[2] = b.x, r[3] = b.y;
+  } else if constexpr (VW == 4 && sizeof(T) == 4) {
     float4 v = *reinterpret_cast<const float4*>(p);
     r[0] = v.x, r[1] = v.y, r[2] = v.z, r[3] = v.w;
   } else if constexpr (VW == 2 && sizeof(T) == 4) {
@@ -97,7 +100,10 @@ __device__ __forceinline__ void vload(T* r, const T* p) {
 }
 template <typename T, int VW>
 __device__ __forceinline__ void vstore(T* p, const T* r) {
-  if constexpr (VW == 4 && sizeof(T) == 4) {
+  if constexpr (VW == 4 && sizeof(T) == 8) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(r[0], r[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(r[2], r[3]);
+  } else if constexpr (VW == 4 && sizeof(T) == 4) {
     *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
   } else if constexpr (VW == 2 && sizeof(T) == 4) {
     *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
@@ -130,9 +136,13 @@ struct RoundUp {
 
 // Per-tile helpers shared by the pipelined and the tensor-core stage kernels.
 // C provides the element shape (D, NP, NF, NFP, NV, NPERM, NK), the tile
-// (ET elements, NT threads), the record sizes and the face-plane stride NKP.
-// Tile buffers: sY [NV][ET][NP], sGF [ET][RECF], sGI [ET][RECI],
-// sN [NV][ET][NKP].
+// (ET elements, NT threads), the record sizes and the face buffer's strides:
+// entry (variable q, element el, face node k) of sN sits at
+// el * SN_EL + k * SN_K + q * SN_Q, either one plane per variable
+// [NV][ET][NKP] (SN_Q = ET * NKP) or the variables of a face node side by side
+// [ET][NKP][NVQ] (SN_Q = 1, NVQ = NV), so that the
+// lifting reads all variables of a node with one vector load.
+// Tile buffers: sY [NV][ET][NP], sGF [ET][RECF], sGI [ET][RECI], sN.
 
 // Issues cp.async gathers of the neighbour traces of every interior face
 // node of the tile whose neighbour lies outside the tile (elements e0 ..
@@ -153,7 +163,7 @@ __device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_
       const T* src = y_in + (int64_t)nbr * NP + nn;
 #pragma unroll
       for (int q = 0; q < NV; ++q) {
-        T* dst = sN + (size_t)(q * ET + el) * C::NKP + k;
+        T* dst = sN + (size_t)el * C::SN_EL + k * C::SN_K + q * C::SN_Q;
         if (sizeof(T) == 4)
           cp_async4(dst, src + q * stride);
         else
@@ -189,7 +199,7 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
 #pragma unroll
     for (int d = 0; d < D; ++d) n[d] = gf[d];
     const T sJ = gf[D];
-    T* slot = sN + (size_t)el * C::NKP + k;  // variable q at slot[q * ET * NKP]
+    T* slot = sN + (size_t)el * C::SN_EL + k * C::SN_K;  // variable q at slot[q * SN_Q]
     T h[NV];
     if (code & kCodeBoundary) {
       const T* B = bmat + (int64_t)nbr * NV * NV;
@@ -210,7 +220,7 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
         for (int q = 0; q < NV; ++q) up[q] = sY[(q * ET + (int)rel) * NP + nn];
       } else {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * ET * C::NKP];
+        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * C::SN_Q];
       }
       const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
       const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
@@ -227,8 +237,15 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
 #pragma unroll
       for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
     }
+    if constexpr (C::SN_Q == 1) {
+      T hv[C::NVQ];
 #pragma unroll
-    for (int q = 0; q < NV; ++q) slot[(size_t)q * ET * C::NKP] = sJ * h[q];
+      for (int q = 0; q < C::NVQ; ++q) hv[q] = q < NV ? sJ * h[q < NV ? q : 0] : (T)0;
+      vstore<T, C::NVQ>(slot, hv);
+    } else {
+#pragma unroll
+      for (int q = 0; q < NV; ++q) slot[(size_t)q * C::SN_Q] = sJ * h[q];
+    }
   }
 }
 
@@ -263,11 +280,15 @@ struct Pipe {
   static constexpr size_t oGF = oY + 2 * (size_t)NV * YSEG;                  // 2 x [ET][RECF]
   static constexpr size_t oGI = oGF + 2 * (size_t)GFB;                        // 2 x [ET][RECI]
   static constexpr size_t oE = RoundUp<oGI + 2 * (size_t)GIB, 128>::v;       // [3][NV][ET][NP]
-  // neighbour traces / face fluxes: one plane per variable, element stride
-  // NKP odd so that reads of one face node across elements hit distinct banks
+  // neighbour traces / face fluxes, the variables of a face node side by
+  // side; element stride NKP (odd) x NVQ so that the elements of a warp read
+  // distinct banks
   static constexpr int NKP = NK | 1;
-  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                    // [NV][ET][NKP]
-  static constexpr size_t oR = RoundUp<oN + (size_t)NV * ET * NKP * sizeof(T), 16>::v;  // [NT/32][5] double
+  static constexpr int NVQ = NV;  // 2-D: three words, no padding (it would cost occupancy)
+  static constexpr int SN_EL = NKP * NVQ, SN_K = NVQ, SN_Q = 1;
+  static constexpr size_t SN_WORDS = (size_t)ET * NKP * NVQ;
+  static constexpr size_t oN = oE + 3 * (size_t)NV * YSEG;                    // [ET][NKP][NVQ]
+  static constexpr size_t oR = RoundUp<oN + SN_WORDS * sizeof(T), 16>::v;   // [NT/32][5] double
   static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
   static_assert(NT % 32 == 0, "threads per block must be a multiple of 32");
   static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
@@ -363,12 +384,11 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
 
   // ---- lifting ----
   {
-    const T* hrow = sN + (size_t)e * C::NKP;
+    const T* hrow = sN + (size_t)e * C::SN_EL;
 #pragma unroll 4
     for (int k = 0; k < NK; ++k) {
-      T hq[NV];
-#pragma unroll
-      for (int q = 0; q < NV; ++q) hq[q] = hrow[(size_t)q * ET * C::NKP + k];
+      T hq[C::NVQ];
+      vload<T, C::NVQ>(hq, hrow + k * C::NVQ);
       T lv[NC];
       load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
 #pragma unroll

@@ -58,6 +58,10 @@ struct C3Cfg {
   static constexpr int NT = 32 * EG * NSPLIT;
   static constexpr int RECF = S::RECF, RECI = S::RECI;
   static constexpr int NKP = NK | 1;
+  // face buffer: the variables of a face node side by side (see stage2.cuh)
+  static constexpr int NVQ = NV;  // 2-D: three words, no padding (it would cost occupancy)
+  static constexpr int SN_EL = NKP * NVQ, SN_K = NVQ, SN_Q = 1;
+  static constexpr size_t SN_WORDS = (size_t)ET * NKP * NVQ;
   static constexpr bool UNROLL = NP <= 16;  // compile-time operator addresses
   static constexpr int OFF_DT = COpsOff<D_, P>::v, OFF_L = OFF_DT + D * NP * NP;
   static constexpr uint32_t YSEG = ET * NP * sizeof(float);
@@ -72,9 +76,9 @@ struct C3Cfg {
   static constexpr size_t oGF = oYT + (size_t)NV * YSEG;                      // 2 x [ET][RECF]
   static constexpr size_t oGI = oGF + 2 * (size_t)GFB;                        // 2 x [ET][RECI]
   static constexpr size_t oN = RoundUp<oGI + 2 * (size_t)GIB, 128>::v;       // [NV][ET][NKP], then dt L [NV][ET][NP]
-  static constexpr size_t oR = RoundUp<oN + (size_t)NV * ET * NKP * 4, 16>::v;
+  static constexpr size_t oR = RoundUp<oN + SN_WORDS * 4, 16>::v;
   static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
-  static_assert(NP <= NKP, "dt L must fit in the face-flux buffer");
+  static_assert((size_t)NV * ET * NP <= SN_WORDS, "dt L must fit in the face-flux buffer");
   static_assert((ET * NP) % 4 == 0, "tile segments must be float4 multiples");
 };
 
@@ -122,9 +126,8 @@ __device__ __forceinline__ void chunk_rhs(const float* sYT, const float* sN, int
   }
 #pragma unroll(C::UNROLL ? NK : 1)
   for (int k = 0; k < NK; ++k) {
-    float h[NV];
-#pragma unroll
-    for (int q = 0; q < NV; ++q) h[q] = sN[(size_t)(q * ET + e) * C::NKP + k];
+    float h[C::NVQ];
+    vload<float, C::NVQ>(h, sN + (size_t)e * C::SN_EL + k * C::NVQ);
 #pragma unroll
     for (int ii = 0; ii < NC; ++ii) {
       if (I0 + ii >= NP) break;

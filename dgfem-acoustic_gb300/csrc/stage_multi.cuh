@@ -48,7 +48,7 @@ constexpr size_t multi_epi_bytes() {
 }
 template <class C>
 constexpr size_t multi_nbuf_bytes() {
-  return (size_t)C::NV * C::ET * C::NKP * 4;
+  return C::SN_WORDS * 4;
 }
 
 struct MultiLayout {

@@ -163,6 +163,9 @@ struct TcCfg {
   static constexpr int NT = 128 * NPART;   // lane quarters x parts
   static constexpr int RECF = S::RECF, RECI = S::RECI;
   static constexpr int NKP = NK | 1;
+  // face buffer: one plane per variable (the face rows read one variable's
+  // face nodes side by side)
+  static constexpr int NVQ = 1, SN_EL = NKP, SN_K = 1, SN_Q = ET * NKP;
   static constexpr int NPP = RoundUpTc<NP, 4>::v;       // volume block width per direction
   static constexpr int KV = D * NPP;                     // volume columns
   static constexpr int KF = RoundUpTc<NK, 4>::v;         // face columns
