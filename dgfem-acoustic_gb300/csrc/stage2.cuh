@@ -144,6 +144,23 @@ struct RoundUp {
 // lifting reads all variables of a node with one vector load.
 // Tile buffers: sY [NV][ET][NP], sGF [ET][RECF], sGI [ET][RECI], sN.
 
+// Face work is split into items of one element face and a run of MC of its
+// NFP nodes; the face's data (neighbour, code, normal, scale, mean-flow
+// component, boundary matrix) is read once per item. FCH, the runs per face,
+// is the smallest divisor of NFP for which the items fill the block (equal
+// runs: measured faster than uneven ones on the 3-D p = 3 kernels).
+constexpr int face_runs(int nfp, int items_per_run, int nt) {
+  for (int d = 1; d <= nfp; ++d)
+    if (nfp % d == 0 && items_per_run * d >= nt) return d;
+  return nfp;
+}
+template <class C>
+struct FaceSplit {
+  static constexpr int FCH = face_runs(C::NFP, C::ET * C::NF, C::NT);
+  static constexpr int MC = C::NFP / FCH;
+  static constexpr int ITEMS = C::ET * C::NF * FCH;
+};
+
 // Issues cp.async gathers of the neighbour traces of every interior face
 // node of the tile whose neighbour lies outside the tile (elements e0 ..
 // e0+ET-1) into sN (the caller commits and waits); traces of neighbours
@@ -151,23 +168,29 @@ struct RoundUp {
 template <class C, typename T>
 __device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_t stride, const int* sGI,
                                               const short* sNb, T* sN, int tid, int64_t e0) {
-  constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
+  constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM;
   constexpr int ET = C::ET, NT = C::NT, RECI = C::RECI;
-  for (int q8 = tid; q8 < ET * NK; q8 += NT) {
-    const int el = q8 / NK, k = q8 - el * NK;
-    const int f = k / NFP, m = k - f * NFP;
+  using FS = FaceSplit<C>;
+  for (int it = tid; it < FS::ITEMS; it += NT) {
+    const int el = it / (NF * FS::FCH), rem = it - el * (NF * FS::FCH);
+    const int f = rem / FS::FCH, ch = rem - f * FS::FCH;
     const int code = sGI[el * RECI + NF + f];
     const int nbr = sGI[el * RECI + f];
-    if (!(code & kCodeBoundary) && (uint64_t)((int64_t)nbr - e0) >= (uint64_t)ET) {
-      const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
-      const T* src = y_in + (int64_t)nbr * NP + nn;
+    if ((code & kCodeBoundary) || (uint64_t)((int64_t)nbr - e0) < (uint64_t)ET) continue;
+    const short* nbt = sNb + ((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP;
+    const T* src0 = y_in + (int64_t)nbr * NP;
+    T* dst0 = sN + (size_t)el * C::SN_EL + f * NFP * C::SN_K;
+#pragma unroll
+    for (int mm = 0; mm < FS::MC; ++mm) {
+      const int m = ch * FS::MC + mm;
+      const T* src = src0 + nbt[m];
+      T* dst = dst0 + m * C::SN_K;
 #pragma unroll
       for (int q = 0; q < NV; ++q) {
-        T* dst = sN + (size_t)el * C::SN_EL + k * C::SN_K + q * C::SN_Q;
         if (sizeof(T) == 4)
-          cp_async4(dst, src + q * stride);
+          cp_async4(dst + q * C::SN_Q, src + q * stride);
         else
-          cp_async8(dst, src + q * stride);
+          cp_async8(dst + q * C::SN_Q, src + q * stride);
       }
     }
   }
@@ -183,15 +206,12 @@ template <class C, typename T>
 __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T* sY, const T* sGF, const int* sGI,
                                             const short* sFm, const short* sNb, T* sN, int tid, T rhoc2, T inv_rho0,
                                             T half_c0, int64_t e0) {
-  constexpr int D = C::D, NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NK = C::NK, NPERM = C::NPERM;
+  constexpr int D = C::D, NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM;
   constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
-  for (int q8 = tid; q8 < ET * NK; q8 += NT) {
-    const int el = q8 / NK, k = q8 - el * NK;
-    const int f = k / NFP;
-    const int node = sFm[k];
-    T um[NV];
-#pragma unroll
-    for (int q = 0; q < NV; ++q) um[q] = sY[(q * ET + el) * NP + node];
+  using FS = FaceSplit<C>;
+  for (int it = tid; it < FS::ITEMS; it += NT) {
+    const int el = it / (NF * FS::FCH), rem = it - el * (NF * FS::FCH);
+    const int f = rem / FS::FCH, ch = rem - f * FS::FCH;
     const int nbr = sGI[el * RECI + f];
     const int code = sGI[el * RECI + NF + f];
     const T* gf = sGF + el * RECF + D * D + f * (D + 1);
@@ -199,52 +219,81 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
 #pragma unroll
     for (int d = 0; d < D; ++d) n[d] = gf[d];
     const T sJ = gf[D];
-    T* slot = sN + (size_t)el * C::SN_EL + k * C::SN_K;  // variable q at slot[q * SN_Q]
-    T h[NV];
-    if (code & kCodeBoundary) {
-      const T* B = bmat + (int64_t)nbr * NV * NV;
+    const T* ye = sY + el * NP;
+    T* srow = sN + (size_t)el * C::SN_EL + f * NFP * C::SN_K;
+    const short* fm = sFm + f * NFP;
+    auto put = [&](int m, const T (&h)[NV]) {
+      T* slot = srow + m * C::SN_K;
+      if constexpr (C::SN_Q == 1) {
+        T hv[C::NVQ];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) {
-        T acc = 0;
-#pragma unroll
-        for (int qq = 0; qq < NV; ++qq) acc += __ldg(B + q * NV + qq) * um[qq];
-        h[q] = acc;
-      }
-    } else {
-      T up[NV];
-      const int64_t rel = (int64_t)nbr - e0;
-      if ((uint64_t)rel < (uint64_t)ET) {
-        const int m = k - f * NFP;
-        const int nn = sNb[((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP + m];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) up[q] = sY[(q * ET + (int)rel) * NP + nn];
+        for (int q = 0; q < C::NVQ; ++q) hv[q] = q < NV ? sJ * h[q < NV ? q : 0] : (T)0;
+        vstore<T, C::NVQ>(slot, hv);
       } else {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * C::SN_Q];
+        for (int q = 0; q < NV; ++q) slot[(size_t)q * C::SN_Q] = sJ * h[q];
       }
+    };
+    if (code & kCodeBoundary) {
+      T B[NV][NV];
+      const T* Bg = bmat + (int64_t)nbr * NV * NV;
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int qq = 0; qq < NV; ++qq) B[q][qq] = __ldg(Bg + q * NV + qq);
+#pragma unroll
+      for (int mm = 0; mm < FS::MC; ++mm) {
+        const int m = ch * FS::MC + mm;
+          const int node = fm[m];
+        T um[NV], h[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) um[q] = ye[q * ET * NP + node];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          T acc = 0;
+#pragma unroll
+          for (int qq = 0; qq < NV; ++qq) acc += B[q][qq] * um[qq];
+          h[q] = acc;
+        }
+        put(m, h);
+      }
+    } else {
+      const int64_t rel = (int64_t)nbr - e0;
+      const bool in_tile = (uint64_t)rel < (uint64_t)ET;
+      const short* nbt = sNb + ((code & kCodeLfMask) * NPERM + ((code >> kCodePermShift) & kCodePermMask)) * NFP;
+      const T* yn = sY + (in_tile ? (int)rel : 0) * NP;
       const T hc = (code & kCodeNegPenalty) ? -half_c0 : half_c0;
       const T* ev0 = sGF + el * RECF + C::S::PHYS_OFF;
       T vn0 = ev0[0] * n[0];
-      #pragma unroll
+#pragma unroll
       for (int d = 1; d < D; ++d) vn0 += ev0[d] * n[d];
-      T avg[NV], dif[NV];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
-      T nv = n[0] * avg[1];
-      #pragma unroll
-      for (int d = 1; d < D; ++d) nv += n[d] * avg[1 + d];
-      h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
+      for (int mm = 0; mm < FS::MC; ++mm) {
+        const int m = ch * FS::MC + mm;
+          const int node = fm[m];
+        T um[NV], up[NV], h[NV];
 #pragma unroll
-      for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
-    }
-    if constexpr (C::SN_Q == 1) {
-      T hv[C::NVQ];
+        for (int q = 0; q < NV; ++q) um[q] = ye[q * ET * NP + node];
+        if (in_tile) {
+          const int nn = nbt[m];
 #pragma unroll
-      for (int q = 0; q < C::NVQ; ++q) hv[q] = q < NV ? sJ * h[q < NV ? q : 0] : (T)0;
-      vstore<T, C::NVQ>(slot, hv);
-    } else {
+          for (int q = 0; q < NV; ++q) up[q] = yn[q * ET * NP + nn];
+        } else {
+          const T* slot = srow + m * C::SN_K;
 #pragma unroll
-      for (int q = 0; q < NV; ++q) slot[(size_t)q * C::SN_Q] = sJ * h[q];
+          for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * C::SN_Q];
+        }
+        T avg[NV], dif[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
+        T nv = n[0] * avg[1];
+#pragma unroll
+        for (int d = 1; d < D; ++d) nv += n[d] * avg[1 + d];
+        h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
+#pragma unroll
+        for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
+        put(m, h);
+      }
     }
   }
 }
