@@ -144,11 +144,13 @@ struct RoundUp {
 // lifting reads all variables of a node with one vector load.
 // Tile buffers: sY [NV][ET][NP], sGF [ET][RECF], sGI [ET][RECI], sN.
 
-// Face work is split into items of one element face and a run of MC of its
-// NFP nodes; the face's data (neighbour, code, normal, scale, mean-flow
-// component, boundary matrix) is read once per item. FCH, the runs per face,
-// is the smallest divisor of NFP for which the items fill the block (equal
-// runs: measured faster than uneven ones on the 3-D p = 3 kernels).
+// Face work is split into items of one element face and MC of its NFP nodes
+// (nodes ch, ch + FCH, ...: the items of neighbouring threads take
+// neighbouring face nodes, so that their writes to sN are consecutive); the
+// face's data (neighbour, code, normal, scale, mean-flow component, boundary
+// matrix) is read once per item. FCH, the items per face, is the smallest
+// divisor of NFP for which the items fill the block (equal items: measured
+// faster than uneven ones on the 3-D p = 3 kernels).
 constexpr int face_runs(int nfp, int items_per_run, int nt) {
   for (int d = 1; d <= nfp; ++d)
     if (nfp % d == 0 && items_per_run * d >= nt) return d;
@@ -182,7 +184,7 @@ __device__ __forceinline__ void gather_traces(const T* __restrict__ y_in, int64_
     T* dst0 = sN + (size_t)el * C::SN_EL + f * NFP * C::SN_K;
 #pragma unroll
     for (int mm = 0; mm < FS::MC; ++mm) {
-      const int m = ch * FS::MC + mm;
+      const int m = mm * FS::FCH + ch;
       const T* src = src0 + nbt[m];
       T* dst = dst0 + m * C::SN_K;
 #pragma unroll
@@ -243,7 +245,7 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
         for (int qq = 0; qq < NV; ++qq) B[q][qq] = __ldg(Bg + q * NV + qq);
 #pragma unroll
       for (int mm = 0; mm < FS::MC; ++mm) {
-        const int m = ch * FS::MC + mm;
+        const int m = mm * FS::FCH + ch;
           const int node = fm[m];
         T um[NV], h[NV];
 #pragma unroll
@@ -269,7 +271,7 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
       for (int d = 1; d < D; ++d) vn0 += ev0[d] * n[d];
 #pragma unroll
       for (int mm = 0; mm < FS::MC; ++mm) {
-        const int m = ch * FS::MC + mm;
+        const int m = mm * FS::FCH + ch;
           const int node = fm[m];
         T um[NV], up[NV], h[NV];
 #pragma unroll
