@@ -181,13 +181,16 @@ def run_gpu(args, rank, world):
         step_ms, kern_ms = S.bench_steps(args.steps, dt, flush_bytes=L2_FLUSH_BYTES, kernel_time=True)
     total_ms = step_ms * args.steps
     total_ms = allmax(total_ms, world)
-    # ---- end-to-end through the C ABI with host buffers ----
-    u_host = np.zeros((4, E * np_))
+    # ---- end-to-end through the C ABI with host buffers (page-locked, as a
+    # user of the library allocates them with dg_host_alloc) ----
+    u_host = pkg.gpu.pinned_empty((4, E * np_))
+    u_host[:] = 0.0
+    u_out = pkg.gpu.pinned_empty((4, E * np_))
     barrier(world)
     t0 = time.perf_counter()
     S.set_state(u_host)
     res, tr = S.run(args.steps, dt)
-    u_out = S.get_state()
+    S.get_state(out=u_out)
     e2e_s = time.perf_counter() - t0
     e2e_s = allmax(e2e_s, world)
     state_bytes = 4 * E * np_ * 8
@@ -214,7 +217,7 @@ def run_gpu(args, rank, world):
                    "l2": "flushed between timed steps (256 MiB write)",
                    "step": "source inject + 4 fused RK4 stages + residual + 8 observers (one CUDA graph)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "note": "dg_set_state + dg_run(K steps, host residual/observer arrays) + dg_get_state"},
+                "note": "dg_set_state + dg_run(K steps, host residual/observer arrays) + dg_get_state, state in pinned host memory"},
         "gpu_launches": int(args.steps * 8),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": "stage_kernel (4 launches per step)",

@@ -1124,6 +1124,23 @@ int dg_kernel_info(dg_ctx* c, int variant, int* out) {
   return DG_OK;
 }
 
+int dg_host_alloc(size_t bytes, void** out) {
+  if (!out) return DG_ERR_ARG;
+  *out = nullptr;
+  if (bytes == 0) return DG_ERR_ARG;
+  if (cudaMallocHost(out, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return DG_ERR_CUDA;
+  }
+  return DG_OK;
+}
+
+int dg_host_free(void* p) {
+  if (!p) return DG_OK;
+  return cudaFreeHost(p) == cudaSuccess ? DG_OK : DG_ERR_CUDA;
+}
+
 int dg_tune_cache_stats(int64_t* hits, int64_t* misses, int64_t* entries) {
   TuneCache& tc = tune_cache();
   std::lock_guard<std::mutex> lk(tc.mu);

@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_kernel_info", "dg_vtu_writer_create", "dg_vtu_write_async",
+           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_host_alloc", "dg_host_free", "dg_kernel_info", "dg_vtu_writer_create", "dg_vtu_write_async",
            "dg_vtu_writer_flush", "dg_vtu_writer_destroy", "dg_vtu_writer_last_error", "dg_vtu_writer_stats", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
            "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench", "dg_batch_set_fused",
@@ -87,6 +87,8 @@ def lib():
         L.dg_vtu_writer_last_error.argtypes = [C.c_void_p]
         L.dg_vtu_writer_last_error.restype = C.c_char_p
         L.dg_vtu_writer_stats.argtypes = [C.c_void_p, P(I64), P(C.c_int)]
+        L.dg_host_alloc.argtypes = [C.c_size_t, P(C.c_void_p)]
+        L.dg_host_free.argtypes = [C.c_void_p]
         L.dg_tune_cache_clear.argtypes = []
         L.dg_tune_cache_clear.restype = None
         L.dg_kernel_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
@@ -114,6 +116,21 @@ def _csr(lists, dtype=np.int64):
 
 class SolverError(RuntimeError):
     pass
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """Uninitialised numpy array in page-locked host memory (dg_host_alloc),
+    freed when the array is garbage-collected."""
+    import weakref
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape))
+    ptr = C.c_void_p()
+    rc = lib().dg_host_alloc(max(1, n) * dtype.itemsize, C.byref(ptr))
+    if rc != 0:
+        raise SolverError("dg_host_alloc: %s" % ERRORS.get(rc, rc))
+    buf = (C.c_char * (max(1, n) * dtype.itemsize)).from_address(ptr.value)
+    weakref.finalize(buf, lib().dg_host_free, ptr.value)
+    return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
 
 
 def tune_cache_stats():
@@ -192,10 +209,15 @@ class Solver:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(4, self.ndof)
         self._ck(lib().dg_set_state(self.h, _dp(u)), "dg_set_state")
 
-    def get_state(self):
-        u = np.zeros((4, self.ndof))
-        self._ck(lib().dg_get_state(self.h, _dp(u)), "dg_get_state")
-        return u
+    def get_state(self, out=None):
+        """State [4][E*Np] in the reference layout; into `out` (float64,
+        C-contiguous, e.g. from pinned_empty) when given."""
+        if out is None:
+            out = np.zeros((4, self.ndof))
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != 4 * self.ndof:
+            raise ValueError("out must be a C-contiguous float64 array of 4 * E * Np values")
+        self._ck(lib().dg_get_state(self.h, _dp(out)), "dg_get_state")
+        return out
 
     def rhs(self, u, dt):
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(4, self.ndof)

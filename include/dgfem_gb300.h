@@ -42,6 +42,7 @@
  */
 #ifndef DGFEM_GB300_H
 #define DGFEM_GB300_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -167,6 +168,13 @@ int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* com
  * DG_ERR_ARG for a variant that does not exist for this element type or
  * precision. */
 int dg_tune(dg_ctx* ctx, int variant);
+
+/* Page-locked (pinned) host memory for the host arrays of dg_set_state,
+ * dg_get_state, dg_run and friends: copies from and to it run at the
+ * host-device link's rate instead of through a staging buffer. No reference
+ * counterpart (the reference has no device). */
+int dg_host_alloc(size_t bytes, void** out);
+int dg_host_free(void* p);
 
 /* The autotuner's result cache (process-wide; keyed by GPU model, dimension,
  * order, precision and the mesh's size class floor(log2(padded elements))).
