@@ -231,6 +231,118 @@ def run_gpu(args, rank, world):
     return line
 
 
+SCALE = dict(name="3D LEE at scale: box [0,4]x[0,2]x[0,2], 1,996,500 tets, p=4", counts=(110, 55, 55),
+             lo=(0.0, 0.0, 0.0), hi=(4.0, 2.0, 2.0), order=4, jitter=0.2, seed=3, v0=(34.0, 0.0, 0.0), rho0=1.225,
+             c0=340.0, cfl=0.5, freq=200.0, amp=0.1, size=0.1, centre=(2.0, 1.0, 1.0), n_obs=4)
+
+
+def scale_sources():
+    """Superposed dipole and quadrupole at the centre, expanded into monopoles
+    as the reference's configuration parser does (src/configParser.cpp:87-115):
+    [x, y, z, size, amp, freq, phase, duration] each."""
+    W = SCALE
+    x, y, z = W["centre"]
+    s, a, f = W["size"], W["amp"], W["freq"]
+    mono = lambda px, py, ph: [px, py, z, s / 2.0, a, f, ph, 1e9]
+    dipole = [mono(x - s, y, 0.0), mono(x + s, y, np.pi)]
+    quad = [mono(x - s, y, 0.0), mono(x + s, y, 0.0), mono(x, y - s, np.pi), mono(x, y + s, np.pi)]
+    return dipole + quad
+
+
+def run_scale(args):
+    """Config 3: one 280 M-DOF instance (FP32), the bandwidth roofline study.
+    Reports the autotuned stage kernel's rate, its HBM fraction, the
+    per-variant stage-kernel times on this mesh, and for the tensor-core
+    kernel its MMA rate (3 TF32 products per operand pair)."""
+    pkg = _pkg()
+    W = SCALE
+    t0 = time.perf_counter()
+    m = pkg.meshgen.box(counts=W["counts"], lo=W["lo"], hi=W["hi"], order=W["order"], jitter=W["jitter"],
+                        seed=W["seed"])
+    bcs = {k: "Absorbing" for k in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")}
+    mesh = dict(dim=3, order=W["order"], xyz=m["xyz"], elem_nodes=m["elem_nodes"],
+                groups=pkg.meshgen.solver_groups(m, bcs))
+    del m
+    gen_s = time.perf_counter() - t0
+    hmin = pkg.meshgen.min_altitude(mesh)
+    dt = W["cfl"] * hmin / ((W["c0"] + np.linalg.norm(W["v0"])) * (2 * W["order"] + 1))
+    srcs = scale_sources()
+    rng = np.random.default_rng(W["seed"])
+    obs = [(rng.uniform(0.4, 3.6), rng.uniform(0.2, 1.8), rng.uniform(0.2, 1.8), 0.05) for _ in range(W["n_obs"])]
+    E, np_ = mesh["elem_nodes"].shape
+    nv = 4
+    dofs = E * np_ * nv
+    x = mesh["xyz"][mesh["elem_nodes"].reshape(-1)]
+    sdofs = [np.nonzero((x[:, 0] - c[0]) ** 2 + (x[:, 1] - c[1]) ** 2 + (x[:, 2] - c[2]) ** 2 < c[3] ** 2)[0]
+             for c in srcs]
+    odofs, ows = [], []
+    for o in obs:
+        d = np.sqrt((x[:, 0] - o[0]) ** 2 + (x[:, 1] - o[1]) ** 2 + (x[:, 2] - o[2]) ** 2)
+        idx = np.nonzero(d < o[3])[0]
+        odofs.append(idx)
+        ows.append(1.0 / (d[idx] ** 2 + 1e-12))
+    del x
+    S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=pkg.gpu.DG_FP32)
+    info = S.info()
+    if args.variant != -2:
+        S.tune(args.variant)
+        info = S.info()
+    S.set_sources(sdofs)
+    n_total = args.warmup + 3 * args.steps + 64
+    times = np.arange(n_total) * dt
+    vals = np.stack([c[4] * np.sin(2 * np.pi * c[5] * times + c[6]) for c in srcs], axis=1)
+    S.set_source_values(vals)
+    S.set_observers(odofs, ows)
+    S.snapshot()
+    S.run(args.warmup, dt)
+    with ClockSampler(0) as clk:
+        step_ms, kern_ms = S.bench_steps(args.steps, dt, flush_bytes=L2_FLUSH_BYTES, kernel_time=True)
+    chosen = info["kernel_variant"]
+    # every offered stage-kernel variant on this mesh (stage kernels only, a few steps each)
+    per_variant = {}
+    for v in [-1] + list(range(8)) + [16, 17] + list(range(32, 40)):
+        if v >= 0 and S.kernel_info(v)[0] == 0:
+            continue
+        S.tune(v)
+        S.run(2, dt)
+        _, km = S.bench_steps(4, dt, flush_bytes=L2_FLUSH_BYTES, kernel_time=True)
+        per_variant[str(v)] = round(km, 4)
+    S.tune(chosen)
+    recf = geometry_record_words(3, 4)
+    alg_bytes = 18 * dofs * 4 + 4 * E * (recf * 4 + 8 * 4)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": dofs * args.steps / (step_ms * args.steps * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic (seeded jittered box mesh, dipole + quadrupole)",
+        "config": {"workload": W["name"], "elements": int(E), "order": W["order"], "n_var": nv, "dofs": int(dofs),
+                   "dt": dt, "mesh_generation_s": round(gen_s, 1), "setup_ms": info["setup_ms"],
+                   "sources": "dipole + quadrupole at (2,1,1), 200 Hz (6 monopoles)", "observers": len(obs)},
+        "kernel_variant": chosen,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel_ms_per_step": kern_ms, "algorithmic_bytes_per_step": int(alg_bytes)},
+        "stage_kernel_ms_per_step": per_variant,
+        "clocks": clk.summary(),
+    }
+    if "16" in per_variant or "17" in per_variant:
+        # MMA work of the tensor-core kernel per step: per tile of 32 elements
+        # three kind::tf32 MMAs of M = 128, N = Np rounded to 16, K = the
+        # padded volume and face columns
+        NP, NK = 35, 4 * 15
+        NN = (NP + 15) // 16 * 16
+        NPP = (NP + 3) // 4 * 4
+        KT = (3 * NPP + (NK + 3) // 4 * 4 + 7) // 8 * 8
+        flops_step = 4 * (E // 32) * 3 * 2 * 128 * NN * KT
+        tc = {}
+        for v in ("16", "17"):
+            if v in per_variant:
+                tc[v] = {"tflops": flops_step / (per_variant[v] * 1e-3) / 1e12, "mma_flops_per_step": flops_step}
+        line["tensor_core"] = tc
+    S.close()
+    return line
+
+
 ENSEMBLE_NAME = "batched ensemble: 256 2-D LEE instances, 1k-50k tris, p in {2,3,4}"
 
 
@@ -462,7 +574,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=-2,
                     help="stage kernel variant (-2: autotuned at setup, -1: baseline kernel, k: pipelined variant k)")
-    ap.add_argument("--workload", default="cube", choices=["cube", "ensemble", "surrogate"])
+    ap.add_argument("--workload", default="cube", choices=["cube", "scale", "ensemble", "surrogate"])
     ap.add_argument("--orders", default="2,3,4",
                     help="ensemble workload: element orders of the instances to keep (profiling subsets)")
     ap.add_argument("--profile", action="store_true",
@@ -483,6 +595,10 @@ def main():
     if args.workload == "ensemble" and args.impl != "reference":
         if rank == 0:
             print(json.dumps(run_ensemble(args)), flush=True)
+        return
+    if args.workload == "scale" and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps(run_scale(args)), flush=True)
         return
     if args.workload == "surrogate" and args.impl != "reference":
         if rank == 0:
