@@ -225,7 +225,7 @@ def run_gpu(args, rank, world):
         "clocks": clk.summary(),
         "setup_ms": info["setup_ms"],
         "kernel_variant": info["kernel_variant"], "kernel_grid": info["kernel_grid"],
-        "kernel_variants": {str(v): S.kernel_info(v) for v in [-1] + list(range(8)) + [16, 17] + list(range(32, 40)) if S.kernel_info(v)[0] > 0},
+        "kernel_variants": {str(v): S.kernel_info(v) for v in [-1] + list(range(8)) + [16, 17, 18] + list(range(32, 40)) if S.kernel_info(v)[0] > 0},
     }
     S.close()
     return line
@@ -300,7 +300,7 @@ def run_scale(args):
     chosen = info["kernel_variant"]
     # every offered stage-kernel variant on this mesh (stage kernels only, a few steps each)
     per_variant = {}
-    for v in [-1] + list(range(8)) + [16, 17] + list(range(32, 40)):
+    for v in [-1] + list(range(8)) + [16, 17, 18] + list(range(32, 40)):
         if v >= 0 and S.kernel_info(v)[0] == 0:
             continue
         S.tune(v)
@@ -325,7 +325,7 @@ def run_scale(args):
         "stage_kernel_ms_per_step": per_variant,
         "clocks": clk.summary(),
     }
-    if "16" in per_variant or "17" in per_variant:
+    if any(v in per_variant for v in ("16", "17", "18")):
         # MMA work of the tensor-core kernel per step: per tile of 32 elements
         # three kind::tf32 MMAs of M = 128, N = Np rounded to 16, K = the
         # padded volume and face columns
@@ -335,7 +335,7 @@ def run_scale(args):
         KT = (3 * NPP + (NK + 3) // 4 * 4 + 7) // 8 * 8
         flops_step = 4 * (E // 32) * 3 * 2 * 128 * NN * KT
         tc = {}
-        for v in ("16", "17"):
+        for v in ("16", "17", "18"):
             if v in per_variant:
                 tc[v] = {"tflops": flops_step / (per_variant[v] * 1e-3) / 1e12, "mma_flops_per_step": flops_step}
         line["tensor_core"] = tc

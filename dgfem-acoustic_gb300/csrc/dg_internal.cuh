@@ -185,12 +185,12 @@ cudaError_t launch_stage2_f64_1d(int order, int variant, const StageArgs<double>
 Stage2Info stage2_info_f32_1d(int order, int variant);
 Stage2Info stage2_info_f64_1d(int order, int variant);
 // Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant ids
-// kTcVariant (2 threads per tile row, 256 per block) and kTcVariant + 1
-// (4 threads per row, 512 per block) of the context's kernel selection.
+// kTcVariant, kTcVariant + 1, kTcVariant + 2 (2, 4 or 8 threads per tile row:
+// 256, 512 or 1024 per block) of the context's kernel selection.
 constexpr int kTcVariant = 16;
-constexpr int kTcVariants = 2;
+constexpr int kTcVariants = 3;
 inline bool is_tc_variant(int v) { return v >= kTcVariant && v < kTcVariant + kTcVariants; }
-inline int tc_npart(int v) { return v == kTcVariant ? 2 : 4; }
+inline int tc_npart(int v) { return 2 << (v - kTcVariant); }  // 2, 4, 8 threads per tile row
 cudaError_t launch_stage_tc(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
                             cudaStream_t s);
 Stage2Info stage_tc_info(int dim, int order, int npart);

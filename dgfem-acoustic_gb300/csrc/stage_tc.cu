@@ -1,7 +1,7 @@
 // Instantiations of the tensor-core stage kernel (FP32 state), 2-D and 3-D,
-// orders 1..4, with 2 or 4 threads per tile row (256 or 512 threads per
-// block). They are offered to the context's kernel selection as variants
-// kTcVariant and kTcVariant + 1 next to the CUDA-core variants.
+// orders 1..4, with 2, 4 or 8 threads per tile row (256, 512 or 1024 threads
+// per block). They are offered to the context's kernel selection as variants
+// kTcVariant .. kTcVariant + 2 next to the CUDA-core variants.
 #include "stage_tc.cuh"
 
 namespace dgk {
@@ -12,8 +12,9 @@ cudaError_t launch_stage_tc(int dim, int order, int npart, const StageArgs<float
                             cudaStream_t s) {
 #define DGK_TC_LAUNCH(D, P)                                                  \
   if (dim == D && order == P)                                                \
-    return npart == 4 ? StageTc<D, P, 4>::launch(a, grid, err, s)            \
-                      : npart == 2 ? StageTc<D, P, 2>::launch(a, grid, err, s) : cudaErrorInvalidValue;
+    return npart == 8   ? StageTc<D, P, 8>::launch(a, grid, err, s)          \
+           : npart == 4 ? StageTc<D, P, 4>::launch(a, grid, err, s)          \
+           : npart == 2 ? StageTc<D, P, 2>::launch(a, grid, err, s) : cudaErrorInvalidValue;
   DGK_TC_CASES(DGK_TC_LAUNCH)
 #undef DGK_TC_LAUNCH
   return cudaErrorInvalidValue;
@@ -30,6 +31,7 @@ Stage2Info stage_tc_info(int dim, int order, int npart) {
   if (dim == D && order == P) {                                   \
     if (npart == 2) return tc_info<D, P, 2>();                    \
     if (npart == 4) return tc_info<D, P, 4>();                    \
+    if (npart == 8) return tc_info<D, P, 8>();                    \
   }
   DGK_TC_CASES(DGK_TC_INFO)
 #undef DGK_TC_INFO

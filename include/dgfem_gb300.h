@@ -90,7 +90,7 @@ typedef struct {
   int64_t penalty_sign_hist[2]; /* interior faces with s_f = -1, +1 */
   int64_t device_bytes;
   double setup_ms;
-  int kernel_variant; /* stage kernel in use: -1 baseline, 0..15 pipelined variant k, 16/17 tensor-core
+  int kernel_variant; /* stage kernel in use: -1 baseline, 0..15 pipelined variant k, 16..18 tensor-core
                          kernel, 32.. constant-operator variant */
   int kernel_grid;    /* blocks of each stage-kernel launch (persistent blocks for variants >= 0) */
   int64_t n_curved;   /* curved elements (high-order nodes off the straight-sided lattice), integrated
@@ -161,9 +161,9 @@ int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* com
  * dg_create does; the environment variable DGFEM_STAGE_VARIANT overrides it
  * there); -1: baseline kernel; k >= 0:
  * pipelined variant k (TMA-staged tiles; the variants differ in output nodes
- * per thread and elements per tile); 16 and 17: tensor-core kernel with 256
- * or 512 threads per block (FP32 contexts only: tcgen05 MMAs with a 3xTF32
- * split, FP32-level results); 32 + k: constant-operator variant k (FP32
+ * per thread and elements per tile); 16, 17, 18: tensor-core kernel with 256,
+ * 512 or 1024 threads per block (FP32 contexts only: tcgen05 MMAs with a
+ * 3xTF32 split, FP32-level results); 32 + k: constant-operator variant k (FP32
  * contexts only: operators in constant memory). Returns
  * DG_ERR_ARG for a variant that does not exist for this element type or
  * precision. */

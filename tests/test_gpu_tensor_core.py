@@ -1,8 +1,8 @@
 """The tensor-core stage kernel (tcgen05, 3xTF32 split, FP32 state) and the
 Euler1 integrator against the CPU oracle, through the C ABI.
 
-The tensor-core kernel is kernel variant 16 (256 threads per block) or 17
-(512 threads per block, each tile row's columns split four ways) of an FP32
+The tensor-core kernel is kernel variant 16, 17 or 18 (256, 512 or 1024
+threads per block: each tile row's columns split 2, 4 or 8 ways) of an FP32
 context. Its products
 keep about 21 mantissa bits (x = tf32 head + fp32 tail, the tail-tail product
 dropped), so it is held to the same bounds as the CUDA-core FP32 kernels: a
@@ -19,6 +19,7 @@ pytestmark = pytest.mark.gpu
 
 TC = 16
 TC4 = 17
+TC8 = 18
 
 
 def _obs_err(tr, ref_obs):
@@ -33,7 +34,7 @@ def _solver(pkg, mesh, ph, prec="fp32"):
     return pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
 
 
-@pytest.mark.parametrize("tc", [TC, TC4])
+@pytest.mark.parametrize("tc", [TC, TC4, TC8])
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
 def test_tc_rhs_matches_oracle(pkg, oracle, dim, p, tc):
@@ -58,7 +59,7 @@ def test_tc_rhs_matches_oracle(pkg, oracle, dim, p, tc):
 def test_tc_not_offered_in_fp64(pkg):
     mesh = _mesh(pkg, 2, 2)
     S = _solver(pkg, mesh, _phys(2), "fp64")
-    for tc in (TC, TC4):
+    for tc in (TC, TC4, TC8):
         with pytest.raises(pkg.gpu.SolverError):
             S.tune(tc)
 
@@ -97,7 +98,7 @@ def _run(pkg, oracle, mesh, ph, prec, variant, nsteps, euler=False):
 
 
 @pytest.mark.parametrize("dim,p,tc", [(2, 2, TC), (2, 3, TC), (2, 4, TC), (3, 2, TC), (3, 3, TC), (3, 4, TC),
-                                      (2, 3, TC4), (3, 3, TC4)])
+                                      (2, 3, TC4), (3, 3, TC4), (3, 4, TC8)])
 def test_tc_run_matches_oracle(pkg, oracle, dim, p, tc):
     mesh = _mesh(pkg, dim, p)
     u, res, tr, ref = _run(pkg, oracle, mesh, _phys(dim), "fp32", tc, 40)
@@ -119,7 +120,7 @@ def test_euler_run_matches_oracle(pkg, oracle, dim, p, prec, variant):
     assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= tol * 10
 
 
-@pytest.mark.parametrize("tc", [TC, TC4])
+@pytest.mark.parametrize("tc", [TC, TC4, TC8])
 def test_tc_many_tiles_per_block(pkg, oracle, tc):
     """A mesh with more tiles than resident blocks, so that every block walks
     several tiles through both halves of its double buffer: one RHS against
