@@ -76,16 +76,20 @@ __device__ __forceinline__ void tmem_st4(uint32_t ta, const uint32_t* v) {
                "r"(v[2]), "r"(v[3])
                : "memory");
 }
-__device__ __forceinline__ void tmem_ld4(uint32_t ta, float* v) {
-  uint32_t r0, r1, r2, r3;
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// 4 accumulator columns of this warp's lane quarter without waiting; the
+// registers are valid after tmem_wait_ld4 on them
+__device__ __forceinline__ void tmem_ld4_async(uint32_t ta, uint32_t* r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(ta)
                : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-  v[0] = __uint_as_float(r0), v[1] = __uint_as_float(r1), v[2] = __uint_as_float(r2), v[3] = __uint_as_float(r3);
 }
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// waits for every outstanding tcgen05.ld of the thread; the registers are
+// operands so that no use of them is scheduled before the wait
+__device__ __forceinline__ void tmem_wait_ld4(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3])::"memory");
+}
 
 // 1-D TMA bulk store shared -> global (bytes % 16 == 0, 16-byte aligned).
 __device__ __forceinline__ void tma_store_1d(void* dst, const void* src, uint32_t bytes) {
@@ -478,14 +482,26 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
       T* r1 = sE + (size_t)(NV * ET + q * ET + e) * NP;        // slot 1 row: acc in, new acc out
       const T* ry = sY + (size_t)(q * ET + e) * NP;            // stage input row (u in stages 1, 5)
       const T* gs = a.snap + q * stride + (e0 + e) * NP;      // residual snapshot row (stage 4)
-      for (int c4 = part; c4 < NN / 4; c4 += NPART) {
+      // this thread's accumulator chunks (columns part*4, (part+NPART)*4, ...
+      // below NP): every load issued first, one wait
+      constexpr int NCH = (NN / 4 + NPART - 1) / NPART;
+      uint32_t dr[NCH][4];
+#pragma unroll
+      for (int t = 0; t < NCH; ++t) {
+        const int c4 = part + t * NPART;
+        if (c4 * 4 < NP) tmem_ld4_async(trow + C::COL_D + c4 * 4, dr[t]);  // warp-uniform condition
+      }
+#pragma unroll
+      for (int t = 0; t < NCH; ++t)
+        if ((part + t * NPART) * 4 < NP) tmem_wait_ld4(dr[t]);
+#pragma unroll
+      for (int t = 0; t < NCH; ++t) {
+        const int c4 = part + t * NPART;
         const int i0 = c4 * 4;
         if (i0 >= NP) break;  // warp-uniform
-        float dv[4];
-        tmem_ld4(trow + C::COL_D + i0, dv);
         T kv[4], x0[4], x1[4], o0[4], o1[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) kv[u] = dte * dv[u];
+        for (int u = 0; u < 4; ++u) kv[u] = dte * __uint_as_float(dr[t][u]);
         switch (stage) {
           case 0:
             store4<NP, VW>(r0, i0, kv);
