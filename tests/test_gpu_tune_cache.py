@@ -28,7 +28,9 @@ S.close()
 """
 
 
-def test_second_context_takes_cached_variant(pkg):
+def test_second_context_takes_cached_variant(pkg, monkeypatch):
+    # the in-process cache only: no cache file from the environment
+    monkeypatch.delenv("DGFEM_TUNE_CACHE", raising=False)
     g = pkg.gpu
     g.tune_cache_clear()
     mesh = _mesh(pkg, 2, 3)
