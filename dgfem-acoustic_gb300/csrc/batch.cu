@@ -1,6 +1,6 @@
 // Batched ensemble of independent solver instances (dg_batch_* in
 // include/dgfem_gb300.h). No counterpart in the reference, which runs one
-// case per process; this is the benchmark spec's batched mode: hundreds of
+// case per process. Here hundreds of
 // independent LEE runs (different meshes, orders, sources, mean flows and time
 // steps) advanced together so that the GPU is filled even when each instance
 // is small.

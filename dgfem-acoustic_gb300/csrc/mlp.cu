@@ -3,7 +3,7 @@
 // observer log-spectra, trained and evaluated on the GPU by the kernels of
 // this file (dg_mlp_* in include/dgfem_gb300.h). It has no counterpart in the
 // reference: the reference answers every parameter query with a full DG run,
-// which remains the fallback and the judge of the network's error.
+// which remains the fallback and the measure of the network's error.
 //
 // Numerics: weights are held in BF16 for the forward and backward passes
 // (FP32 master copies for the optimiser), activations and gradients in FP32,

@@ -8,7 +8,7 @@ BF16 weights, FP32 accumulation) that is trained and evaluated on the GPU by
 the project's own kernels (gpu.Network, csrc/mlp.cu).
 
 The reference has no counterpart: it answers every query with a DG run. DG
-stays the judge and the fallback here: the training and test targets come
+stays the measure of the network's error and its fallback here: the training and test targets come
 from batched DG runs, and a query whose estimated spectral error exceeds the
 bound is re-run through DG. The error estimate is the disagreement of two
 independently trained networks, scaled so that it covers the true error of
