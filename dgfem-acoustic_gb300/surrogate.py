@@ -10,9 +10,10 @@ the project's own kernels (gpu.Network, csrc/mlp.cu).
 The reference has no counterpart: it answers every query with a DG run. DG
 stays the measure of the network's error and its fallback here: the training and test targets come
 from batched DG runs, and a query whose estimated spectral error exceeds the
-bound is re-run through DG. The error estimate is the disagreement of two
-independently trained networks, scaled so that it covers the true error of
-95 % of a calibration split.
+bound is re-run through DG. The error estimate is the spread of independently
+trained networks around their mean (two by default, four in the shipped
+model), scaled so that it covers the true error of 95 % of a calibration
+split.
 
 Targets: the last power-of-two samples of the observer pressure trace of
 STEPS RK4 steps (the settled part: the first samples hold the wave-front
