@@ -51,6 +51,11 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t
       : "memory");
 }
 
+// Bulk prefetch of bytes at p into L2 (no completion to wait for).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Bounded wait for the phase with the given parity; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
@@ -361,15 +366,18 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
   const int64_t stride = a.stride;
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
-  const int e = tid / NSPLIT, s = tid - (tid / NSPLIT) * NSPLIT;
+  // a block larger than this shape's NT (the mixed-order kernel) leaves its
+  // other threads idle in this tile; they only take part in the barriers
+  const bool active = tid < C::NT;
+  const int e = active ? tid / NSPLIT : 0, s = active ? tid - (tid / NSPLIT) * NSPLIT : 0;
   const int i0 = s * NC;
   // ---- neighbour traces: asynchronous gathers into sN ----
-  gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
+  if (active) gather_traces<C, T>(a.y_in, stride, sGI, sNb, sN, tid, e0);
   cp_async_commit();
 
   // ---- volume term for this thread's nodes ----
   T Lv[NC][NV];
-  {
+  if (active) {
     T W[D][NC][NV];
 #pragma unroll
     for (int r = 0; r < D; ++r)
@@ -430,11 +438,11 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
   __syncthreads();
 
   // ---- face numerical fluxes (in place of the gathered traces) ----
-  face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
+  if (active) face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
   __syncthreads();
 
   // ---- lifting ----
-  {
+  if (active) {
     const T* hrow = sN + (size_t)e * C::SN_EL;
 #pragma unroll 4
     for (int k = 0; k < NK; ++k) {
@@ -449,9 +457,10 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
     }
   }
 
-  curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
+  if (active) curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
   // ---- RK update from registers (vectorised when the node chunk allows) ----
   if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity)) ok = false;
+  if (!active) return;
   const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
   const T* ea = sE + (size_t)NV * ET * NP;
   const T* es = sE + (size_t)2 * NV * ET * NP;

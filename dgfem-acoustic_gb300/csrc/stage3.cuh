@@ -150,10 +150,6 @@ __device__ __forceinline__ void chunk_dispatch(int s, const float* sYT, const fl
   }
 }
 
-__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 template <int D, int P, int NC_, int EG_>
 __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const StageArgs<float> a, int* err) {
   using C = C3Cfg<D, P, NC_, EG_>;

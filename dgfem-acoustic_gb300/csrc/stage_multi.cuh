@@ -5,10 +5,12 @@
 // kernel advances all of them in one launch: its blocks take tiles from a
 // work queue over every order's tiles (an atomic counter; order after order)
 // and run each tile with the pipelined kernel's per-tile code for that order
-// (pipe_tile in stage2.cuh), at 128 threads per block for every order:
-//   p = 2: 64 elements per tile, 3 nodes per thread;
-//   p = 3: 32 elements per tile, 3 nodes per thread;
-//   p = 4: 32 elements per tile, 4 nodes per thread.
+// (pipe_tile in stage2.cuh) with that order's own tile shape, the shape of
+// its fastest pipelined variant; the block has the largest shape's thread
+// count (160) and the threads past a shape's count idle in its tiles:
+//   p = 2: 64 elements per tile, 3 nodes per thread, 128 threads;
+//   p = 3: 32 elements per tile, 2 nodes per thread, 160 threads;
+//   p = 4: 32 elements per tile, 5 nodes per thread, 96 threads.
 // Every order's reference operators sit in shared memory. The tile buffers
 // are two fixed slots sized for the largest order (consecutive queue items
 // may be of different orders; the next item's stage input and geometry
@@ -24,9 +26,11 @@
 namespace dgk {
 
 using MultiC2 = Pipe<float, 2, 2, 3, 64>;
-using MultiC3 = Pipe<float, 2, 3, 3, 32>;
-using MultiC4 = Pipe<float, 2, 4, 4, 32>;
-constexpr int kMultiNT = 128;
+using MultiC3 = Pipe<float, 2, 3, 2, 32>;
+using MultiC4 = Pipe<float, 2, 4, 5, 32>;
+constexpr int kMultiNT = 160;
+// blocks per SM the register budget is set for (the shared memory's limit)
+constexpr int kMultiMinBlocks = 4;
 
 template <typename A, typename B>
 constexpr A cmax(A x, B y) {
@@ -66,12 +70,14 @@ struct MultiLayout {
   static constexpr size_t oN = RoundUp<oE + EPI, 128>::v;
   static constexpr size_t NBUF =
       cmax(cmax(multi_nbuf_bytes<MultiC2>(), multi_nbuf_bytes<MultiC3>()), multi_nbuf_bytes<MultiC4>());
-  static constexpr size_t oR = RoundUp<oN + NBUF, 16>::v;  // [orders][warps][5] double
-  static constexpr size_t bytes = oR + (size_t)kMultiOrders * (kMultiNT / 32) * 5 * sizeof(double);
+  static constexpr size_t oR = RoundUp<oN + NBUF, 16>::v;  // [warps][5] double
+  static constexpr size_t bytes = oR + (size_t)(kMultiNT / 32) * 5 * sizeof(double);
 };
 
-static_assert(MultiC2::NT == kMultiNT && MultiC3::NT == kMultiNT && MultiC4::NT == kMultiNT,
-              "every order runs at the same block size");
+static_assert(MultiC2::NT <= kMultiNT && MultiC3::NT <= kMultiNT && MultiC4::NT <= kMultiNT,
+              "the block holds every order's tile shape");
+static_assert(kMultiNT % 32 == 0 && MultiC2::NT % 32 == 0 && MultiC3::NT % 32 == 0 && MultiC4::NT % 32 == 0,
+              "idle threads of a tile are whole warps");
 
 // Operator tables of one order in shared memory (same relative layout as in
 // the order's pipelined kernel).
@@ -158,7 +164,7 @@ __device__ __forceinline__ void multi_run_tile(const StageArgs<float>& a, int ti
                       nepi, tid, ok, racc);
 }
 
-__global__ void __launch_bounds__(kMultiNT) stage_multi_kernel(const MultiArgs m, int* err) {
+__global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(const MultiArgs m, int* err) {
   using L = MultiLayout;
   extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::oBar);  // [0],[1]: slots, [2]: RK operands
@@ -195,14 +201,43 @@ __global__ void __launch_bounds__(kMultiNT) stage_multi_kernel(const MultiArgs m
   // thread 0: slots (bits 0, 1) and RK operands (bit 2) armed and not yet
   // observed complete, drained on exit
   uint32_t pend = 0;
+  // thread 0 claims items one ahead of the prefetch: the queue's atomic
+  // round trip overlaps a tile's work instead of delaying the next copy
+  int ahead = 0;
   if (tid == 0) {
     const int first = (int)atomicAdd(m.queue, 1u);
     *sItem = first;
-    if (first < m.ntiles_total) issue(first, 0), pend = 1u;
+    if (first < m.ntiles_total) {
+      issue(first, 0), pend = 1u;
+      ahead = (int)atomicAdd(m.queue, 1u);
+    }
   }
   __syncthreads();
 
-  ResAcc<float> r2, r3, r4;
+  // stage 4: racc holds the residual sums of order rg; a block's items come
+  // in order after order, so each order's row is written once, when the
+  // block moves on to the next order or finishes (orders bit-set in wrote)
+  ResAcc<float> racc;
+  int rg = -1;
+  unsigned wrote = 0;
+  auto put_row = [&](int g, bool zero) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      double v = zero ? 0.0 : racc.get(c, m.g[g].c0sq);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if ((tid & 31) == 0) sRed[(tid >> 5) * 5 + c] = v;
+    }
+    __syncthreads();
+    if (tid < 5) {
+      double v = 0.0;
+      for (int w = 0; w < kMultiNT / 32; ++w) v += sRed[w * 5 + tid];
+      m.g[g].partials[blockIdx.x * 5 + tid] = v;
+    }
+    __syncthreads();
+    racc = ResAcc<float>();
+    wrote |= 1u << g;
+  };
   bool ok = true;
   int it = 0;
   for (;; ++it) {
@@ -217,11 +252,18 @@ __global__ void __launch_bounds__(kMultiNT) stage_multi_kernel(const MultiArgs m
     }
     int tile;
     const int g = multi_slot(m, item, &tile);
+    if (stage == 4 && g != rg) {  // block-uniform
+      if (rg >= 0) put_row(rg, false);
+      rg = g;
+    }
     if (tid == 0) {
       fence_proxy_async();
-      const int next = (int)atomicAdd(m.queue, 1u);
+      const int next = ahead;
       *sItem = next;
-      if (next < m.ntiles_total) issue(next, b ^ 1), pend |= 1u << (b ^ 1);
+      if (next < m.ntiles_total) {
+        issue(next, b ^ 1), pend |= 1u << (b ^ 1);
+        ahead = (int)atomicAdd(m.queue, 1u);
+      }
       if (nepi > 0) {
         pend |= 4u;
         if (g == 0) multi_issue_epi<MultiC2>(m.g[0], tile, sE, nepi, &bar[2]);
@@ -231,11 +273,11 @@ __global__ void __launch_bounds__(kMultiNT) stage_multi_kernel(const MultiArgs m
     }
     unsigned char* slot = slots + (size_t)b * L::SLOT;
     if (g == 0)
-      multi_run_tile<MultiC2>(m.g[0], tile, slot, sE, sN, ops2, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, r2);
+      multi_run_tile<MultiC2>(m.g[0], tile, slot, sE, sN, ops2, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     else if (g == 1)
-      multi_run_tile<MultiC3>(m.g[1], tile, slot, sE, sN, ops3, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, r3);
+      multi_run_tile<MultiC3>(m.g[1], tile, slot, sE, sN, ops3, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     else
-      multi_run_tile<MultiC4>(m.g[2], tile, slot, sE, sN, ops4, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, r4);
+      multi_run_tile<MultiC4>(m.g[2], tile, slot, sE, sN, ops4, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     if (tid == 0 && ok) pend &= ~4u;  // the RK operands arrived (waited inside the tile)
     if (__syncthreads_or(!ok)) {      // buffers of this item are free again
       ok = false;
@@ -253,28 +295,10 @@ __global__ void __launch_bounds__(kMultiNT) stage_multi_kernel(const MultiArgs m
   if (stage == 4) {
     // residual partial sums per order (one row per block in each order's
     // partials array; a block that ran no tile of an order writes zeros)
+    if (rg >= 0) put_row(rg, false);
 #pragma unroll
-    for (int g = 0; g < kMultiOrders; ++g) {
-      if (m.g[g].ntiles == 0) continue;
-      const ResAcc<float>& r = g == 0 ? r2 : (g == 1 ? r3 : r4);
-#pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        double v = r.get(c, m.g[g].c0sq);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if ((tid & 31) == 0) sRed[(g * (kMultiNT / 32) + (tid >> 5)) * 5 + c] = v;
-      }
-    }
-    __syncthreads();
-    if (tid < 5) {
-#pragma unroll
-      for (int g = 0; g < kMultiOrders; ++g) {
-        if (m.g[g].ntiles == 0) continue;
-        double v = 0.0;
-        for (int w = 0; w < kMultiNT / 32; ++w) v += sRed[(g * (kMultiNT / 32) + w) * 5 + tid];
-        m.g[g].partials[blockIdx.x * 5 + tid] = v;
-      }
-    }
+    for (int g = 0; g < kMultiOrders; ++g)
+      if (m.g[g].ntiles > 0 && !(wrote & (1u << g))) put_row(g, true);
   }
 }
 
