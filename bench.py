@@ -456,7 +456,7 @@ SURROGATE_PATH = os.path.join(ROOT, "dgfem-acoustic_gb300", "data", "surrogate.n
 
 def run_surrogate(args, n_dg=256, bound_db=1.0):
     """The learned spectral surrogate against DG: query throughput of the
-    surrogate (both networks, host arrays in and out) on the 2,000 held-out
+    surrogate (all its networks, host arrays in and out) on the 2,000 held-out
     parameter draws, the batched DG path's query throughput on the first
     n_dg of them (same mesh and step count the targets came from), and the
     surrogate's spectral error against those DG answers."""
@@ -480,12 +480,13 @@ def run_surrogate(args, n_dg=256, bound_db=1.0):
     delivered = S.rms_db(spec, Y)
     return {"metric": "surrogate spectral queries/s", "value": q_s, "unit": "queries/s", "steps": args.steps,
             "warmup": args.warmup, "dtype": "bf16 weights, f32 accumulate",
-            "config": {"workload": "learned surrogate: 6 -> 4x256 GELU -> 4x128 log-PSD, 2 networks",
+            "config": {"workload": "learned surrogate: 6 -> 4x256 GELU -> 4x128 log-PSD, %d networks" % len(sur.nets),
                        "queries": len(P), "dg_grid": sur.grid, "dg_steps": sur.steps},
             "dg": {"value": n_dg / dg_s, "unit": "queries/s", "sample": "%d held-out draws, batched FP32 DG" % n_dg},
             "speedup_over_dg": q_s / (n_dg / dg_s),
             "heldout": {"queries": n_dg, "bound_db": bound_db, "rms_db_median": float(np.median(err)),
-                        "rms_db_p95": float(np.quantile(err, 0.95)), "accepted_fraction": float(acc.mean()),
+                        "rms_db_p95": float(np.quantile(err, 0.95)),
+                        "within_bound_fraction": float(np.mean(err <= bound_db)), "accepted_fraction": float(acc.mean()),
                         "accepted_rms_db_max": float(err[acc].max()) if acc.any() else None,
                         "delivered_rms_db_max": float(delivered.max()),
                         "rerun_through_dg": int(from_dg.sum())}}

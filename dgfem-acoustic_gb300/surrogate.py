@@ -11,25 +11,26 @@ The reference has no counterpart: it answers every query with a DG run. DG
 stays the measure of the network's error and its fallback here: the training and test targets come
 from batched DG runs, and a query whose estimated spectral error exceeds the
 bound is re-run through DG. The error estimate is the spread of independently
-trained networks around their mean (two by default, four in the shipped
-model), scaled so that it covers the true error of 95 % of a calibration
-split.
+trained networks around their mean (four by default), scaled so that it
+covers the true error of 95 % of a calibration split.
 
 Targets: the last power-of-two samples of the observer pressure trace of
 STEPS RK4 steps (the settled part: the first samples hold the wave-front
-arrival), Hann-tapered and power-normalised, go through the project's
-restatement of the reference's PSD_spec (host.spectra: mean removed,
-one-sided periodogram, src/fft.cpp:183-227); the linear power is averaged
-over 128 bins of the source-frequency axis nu = f'/f in [0, NU_MAX)
-(interpolated at the bin centre where a bin holds no FFT line; bin_frequencies
-maps them back to Hz) and expressed in dB re (20 uPa)^2, floored
-DYN_RANGE_DB below each observer's peak bin. The taper replaces the
-rectangular window's leakage pattern, which oscillates with f times the
-window length (and so with f, p and M) faster than the parameter sampling
-resolves, by a compact main lobe; the relative axis keeps the tone at nu = 1
-for every query, so that the network learns its level and lobe shape rather
-than a peak sliding across fixed bins. Instances use one fixed jittered GRID x GRID mesh per order, so the
-spectrum is a function of the six parameters alone.
+arrival), Hann-tapered, power-normalised and zero-padded eightfold, go
+through the project's restatement of the reference's PSD_spec (host.spectra:
+mean removed, one-sided periodogram, src/fft.cpp:183-227); the linear power
+is averaged over 128 bins of the source-frequency axis nu = f'/f in
+[0, NU_MAX) (bin means of the piecewise-linear PSD; bin_frequencies maps
+them back to Hz) and expressed in dB re (20 uPa)^2, floored DYN_RANGE_DB
+below each observer's peak bin. The taper replaces the rectangular window's
+leakage pattern by a compact main lobe; the relative axis keeps the tone at
+nu = 1 for every query, so that the network learns its level and lobe shape
+rather than a peak sliding across fixed bins; the padding and the bin
+integrals make each bin a smooth function of the tone's position between
+FFT lines (without them the tone's bin level moves by up to 1.4 dB with f
+times the record length, faster than the parameter sampling resolves).
+Instances use one fixed jittered GRID x GRID mesh per order, so the spectrum
+is a function of the six parameters alone.
 """
 import importlib
 import math
@@ -41,6 +42,7 @@ WIDTHS = [6, 256, 256, 256, 256, 512]
 N_OBS, N_BINS = 4, 128
 NU_MAX = 4.0  # bins span [0, NU_MAX) source-frequency multiples
 DYN_RANGE_DB = 30.0
+ZERO_PAD = 8  # FFT length / analysed samples
 STEPS = 3000
 GRID = 25
 MESH_SEEDS = {2: 502, 3: 503, 4: 504}
@@ -84,24 +86,31 @@ def bin_frequencies(f):
 def log_psd_bins(trace, dt, f):
     """128-bin log-PSD (dB re (20 uPa)^2) of one pressure trace on the
     source-frequency axis nu = f'/f in [0, NU_MAX): the last power-of-two
-    samples (the settled part of the run), Hann-tapered and
-    power-normalised, through the PSD_spec restatement."""
+    samples n (the settled part of the run), their Hann-weighted mean
+    removed, Hann-tapered, power-normalised and zero-padded to ZERO_PAD * n
+    samples, through the PSD_spec restatement (rescaled to the unpadded
+    segment's PSD level); each bin is the mean over its frequency interval
+    of the piecewise-linear PSD between the FFT lines."""
     tr = np.asarray(trace, dtype=np.float64)
     n = 1
     while n * 2 <= len(tr):
         n *= 2
     seg = tr[len(tr) - n:]
     w = 0.5 * (1.0 - np.cos(2 * np.pi * np.arange(n) / (n - 1)))
-    seg = (seg - seg.mean()) * w / math.sqrt(np.mean(w * w))
-    _, psd = _pkg().host.spectra(seg.astype(np.float32), dt)
-    fl, P = psd[:, 0], psd[:, 1]
+    x = np.zeros(ZERO_PAD * n)
+    # a zero-mean padded record: PSD_spec's own mean removal changes nothing
+    x[:n] = (seg - np.sum(seg * w) / np.sum(w)) * w / math.sqrt(np.mean(w * w))
+    _, psd = _pkg().host.spectra(x.astype(np.float32), dt)
+    m = ZERO_PAD * n
+    fl, P = psd[:, 0], psd[:, 1] * (ZERO_PAD * ZERO_PAD * (n - 1) / (m - 1))
     edges = np.arange(N_BINS + 1) * (NU_MAX / N_BINS) * f
-    idx = np.searchsorted(edges, fl, side="right") - 1
-    ok = (idx >= 0) & (idx < N_BINS)
-    s = np.bincount(idx[ok], weights=P[ok], minlength=N_BINS)
-    c = np.bincount(idx[ok], minlength=N_BINS)
-    centres = 0.5 * (edges[:-1] + edges[1:])
-    out = np.where(c > 0, s / np.maximum(c, 1), np.interp(centres, fl, P))
+    # exact integrals of the piecewise-linear PSD up to each bin edge
+    C = np.concatenate([[0.0], np.cumsum(0.5 * (P[1:] + P[:-1]) * np.diff(fl))])
+    i = np.clip(np.searchsorted(fl, edges, side="right") - 1, 0, len(fl) - 2)
+    xe = np.clip(edges, fl[0], fl[-1])
+    pe = P[i] + (xe - fl[i]) / (fl[i + 1] - fl[i]) * (P[i + 1] - P[i])
+    Ce = C[i] + (xe - fl[i]) * 0.5 * (P[i] + pe)
+    out = np.diff(Ce) / np.diff(edges)
     peak = out.max()
     out = np.maximum(out, peak * 10 ** (-DYN_RANGE_DB / 10) if peak > 0 else 1e-30)
     return 10 * np.log10(out / (2e-5) ** 2)
@@ -157,7 +166,7 @@ def rms_db(a, b):
 
 
 class Surrogate:
-    """Independently trained networks (two by default), target normalisation
+    """Independently trained networks (four by default), target normalisation
     and the calibrated error estimate (the members' spread)."""
 
     def __init__(self, params_list, mu, sigma, scale=1.0, grid=GRID, steps=STEPS, device=0):
@@ -172,8 +181,8 @@ class Surrogate:
             self.nets.append(net)
 
     @classmethod
-    def fit(cls, params, targets, n_models=2, steps=20000, batch=256, lr=2e-3, lr_final=2e-5, seed=0, grid=GRID,
-            dg_steps=STEPS, weight_decay=0.0, device=0):
+    def fit(cls, params, targets, n_models=4, steps=10000, batch=256, lr=4e-3, lr_final=2e-5, seed=0, grid=GRID,
+            dg_steps=STEPS, weight_decay=0.1, device=0):
         x = features(params)
         y = np.asarray(targets, dtype=np.float64).reshape(len(x), -1)
         mu = y.mean(axis=0)

@@ -7,7 +7,7 @@
 2. Runs every row through the batched DG path (FP32, 3000 RK4 steps, one
    fixed jittered mesh per order) and turns the observer pressure traces into
    128-bin log-PSD targets (surrogate.dg_spectra).
-3. Trains two networks on 18,000 training rows (GPU kernels of csrc/mlp.cu),
+3. Trains four networks on 18,000 training rows (GPU kernels of csrc/mlp.cu),
    calibrates the error estimate on the remaining 2,000 training rows, and
    evaluates on the held-out rows: true RMS dB error per query, the queries
    accepted under the 1 dB bound, and throughput against DG.
@@ -32,12 +32,13 @@ def main():
     ap.add_argument("--n-train", type=int, default=20000)
     ap.add_argument("--n-test", type=int, default=2000)
     ap.add_argument("--n-calib", type=int, default=2000)
-    ap.add_argument("--train-steps", type=int, default=60000)
+    ap.add_argument("--train-steps", type=int, default=10000)
+    ap.add_argument("--lr", type=float, default=4e-3)
     ap.add_argument("--dg-steps", type=int, default=3000)
     ap.add_argument("--grid", type=int, default=25)
     ap.add_argument("--bound-db", type=float, default=1.0)
-    ap.add_argument("--models", type=int, default=2)
-    ap.add_argument("--weight-decay", type=float, default=0.0)
+    ap.add_argument("--models", type=int, default=4)
+    ap.add_argument("--weight-decay", type=float, default=0.1)
     args = ap.parse_args()
     sys.path.insert(0, ROOT)
     pkg = importlib.import_module("dgfem-acoustic_gb300")
@@ -45,7 +46,7 @@ def main():
     os.makedirs(args.out, exist_ok=True)
     rep = {"n_train": args.n_train, "n_test": args.n_test, "n_calib": args.n_calib, "dg_steps": args.dg_steps,
            "grid": args.grid, "bound_db": args.bound_db, "models": args.models, "weight_decay": args.weight_decay,
-           "train_steps": args.train_steps}
+           "train_steps": args.train_steps, "lr": args.lr}
 
     P_train = S.draw_params(args.n_train, 5)
     P_test = S.draw_params(args.n_test, 6)
@@ -58,7 +59,7 @@ def main():
 
     nfit = args.n_train - args.n_calib
     t0 = time.perf_counter()
-    sur = S.Surrogate.fit(P_train[:nfit], Y_train[:nfit], n_models=args.models, steps=args.train_steps,
+    sur = S.Surrogate.fit(P_train[:nfit], Y_train[:nfit], n_models=args.models, steps=args.train_steps, lr=args.lr,
                           grid=args.grid, dg_steps=args.dg_steps, weight_decay=args.weight_decay)
     rep["train_s"] = time.perf_counter() - t0
     rep["final_train_loss"] = [float(np.mean(l[-200:])) for l in sur.train_losses]
