@@ -929,7 +929,10 @@ int dg_get_state(dg_ctx* c, double* u) {
 }
 
 int dg_set_sources(dg_ctx* c, int n_src, const int64_t* offsets, const int64_t* dofs) {
-  if (!c || n_src < 0 || (n_src > 0 && (!offsets || !dofs))) return DG_ERR_ARG;
+  if (!c || n_src < 0 || (n_src > 0 && !offsets)) return DG_ERR_ARG;
+  // sources may cover no dof at all (a radius with no node inside): then
+  // dofs may be null
+  if (n_src > 0 && offsets[n_src] > 0 && !dofs) return fail(c, DG_ERR_ARG, "dg_set_sources: dofs is null");
   // unique internal dofs, each with the ordered list of sources covering it
   std::map<int64_t, std::vector<int>> cover;
   const int64_t ndof = c->E * c->np;
@@ -983,7 +986,9 @@ int dg_set_source_values(dg_ctx* c, int64_t n_steps, const double* values) {
 }
 
 int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t* dofs, const double* weights) {
-  if (!c || n_obs < 0 || (n_obs > 0 && (!offsets || !dofs || !weights))) return DG_ERR_ARG;
+  if (!c || n_obs < 0 || (n_obs > 0 && !offsets)) return DG_ERR_ARG;
+  if (n_obs > 0 && offsets[n_obs] > 0 && (!dofs || !weights))
+    return fail(c, DG_ERR_ARG, "dg_set_observers: dofs or weights is null");
   for (void* p : {(void*)c->d_obs_dof, (void*)c->d_obs_off, (void*)c->d_obs_w})
     if (p) cudaFree(p);
   c->d_obs_dof = nullptr, c->d_obs_off = nullptr, c->d_obs_w = nullptr;

@@ -8,11 +8,15 @@ BF16 weights, FP32 accumulation) that is trained and evaluated on the GPU by
 the project's own kernels (gpu.Network, csrc/mlp.cu).
 
 The reference has no counterpart: it answers every query with a DG run. DG
-stays the measure of the network's error and its fallback here: the training and test targets come
-from batched DG runs, and a query whose estimated spectral error exceeds the
-bound is re-run through DG. The error estimate is the spread of independently
-trained networks around their mean (four by default), scaled so that it
-covers the true error of 95 % of a calibration split.
+stays the measure of the network's error and its fallback here: the
+training and test targets come from batched DG runs, and a query whose
+estimated spectral error is above its bound's acceptance threshold is re-run
+through DG. The estimate comes from an error network (6 -> 2 x 128 GELU -> 1,
+the same kernels) trained on the logarithm of out-of-fold errors: networks
+trained like the members, each without one fold of the training rows,
+predict the fold they did not see. A calibration split's estimates and true
+errors set each bound's threshold: the largest estimate under which at most
+5 % of the accepted calibration queries exceed the bound.
 
 Targets: the last power-of-two samples of the observer pressure trace of
 STEPS RK4 steps (the settled part: the first samples hold the wave-front
@@ -46,6 +50,10 @@ ZERO_PAD = 8  # FFT length / analysed samples
 STEPS = 3000
 GRID = 25
 MESH_SEEDS = {2: 502, 3: 503, 4: 504}
+ERR_WIDTHS = [6, 128, 128, 1]  # the error network
+ERR_STEPS, ERR_LR, ERR_WEIGHT_DECAY = 4000, 2e-3, 0.01
+RISK = 0.05  # largest share of accepted calibration queries above the bound
+MIN_ACCEPT = 20  # calibration queries an acceptance threshold rests on
 
 
 def _pkg():
@@ -165,41 +173,99 @@ def rms_db(a, b):
     return np.sqrt(np.mean(d * d, axis=1))
 
 
-class Surrogate:
-    """Independently trained networks (four by default), target normalisation
-    and the calibrated error estimate (the members' spread)."""
+def accept_threshold(est, err, bound_db, risk=None, min_count=None):
+    """Acceptance threshold on the estimated error for a bound: the largest
+    calibration estimate t such that, of the calibration queries with an
+    estimate <= t (at least min_count of them), at most the share `risk` has
+    a true error above bound_db; +inf when the whole calibration split meets
+    that, -inf when no prefix does (every query goes to DG)."""
+    risk = RISK if risk is None else risk
+    min_count = MIN_ACCEPT if min_count is None else min_count
+    est = np.asarray(est, dtype=np.float64).reshape(-1)
+    err = np.asarray(err, dtype=np.float64).reshape(-1)
+    if est.size == 0:
+        return -np.inf
+    o = np.argsort(est, kind="stable")
+    es = est[o]
+    n = np.arange(1, es.size + 1)
+    above = np.cumsum(err[o] > bound_db)
+    # a threshold between two distinct estimates (ties stay together)
+    ok = (above <= risk * n) & (n >= min_count) & np.append(es[1:] > es[:-1], True)
+    if not ok.any():
+        return -np.inf
+    k = int(np.nonzero(ok)[0][-1])
+    return np.inf if k == es.size - 1 else float(es[k])
 
-    def __init__(self, params_list, mu, sigma, scale=1.0, grid=GRID, steps=STEPS, device=0):
+
+class Surrogate:
+    """Independently trained networks (four by default) whose mean answers a
+    query, the target normalisation, the error network (the query's RMS
+    error in dB, learned from out-of-fold errors of networks trained like
+    the members) and a calibration split's estimates and true errors, which
+    set each bound's acceptance threshold (accept_threshold)."""
+
+    def __init__(self, params_list, mu, sigma, err_params, err_mu, err_sigma, calib_est=None, calib_err=None,
+                 grid=GRID, steps=STEPS, device=0):
         self.mu = np.asarray(mu, dtype=np.float32)
         self.sigma = float(sigma)
-        self.scale = float(scale)
+        self.err_mu, self.err_sigma = float(err_mu), float(err_sigma)
+        self.calib_est = np.zeros(0) if calib_est is None else np.asarray(calib_est, dtype=np.float64)
+        self.calib_err = np.zeros(0) if calib_err is None else np.asarray(calib_err, dtype=np.float64)
         self.grid, self.steps = int(grid), int(steps)  # the DG runs the targets came from
+        gpu = _pkg().gpu
         self.nets = []
         for p in params_list:
-            net = _pkg().gpu.Network(WIDTHS, device=device)
+            net = gpu.Network(WIDTHS, device=device)
             net.set_params(p)
             self.nets.append(net)
+        self.err_net = gpu.Network(ERR_WIDTHS, device=device)
+        self.err_net.set_params(err_params)
 
     @classmethod
     def fit(cls, params, targets, n_models=4, steps=10000, batch=256, lr=4e-3, lr_final=2e-5, seed=0, grid=GRID,
-            dg_steps=STEPS, weight_decay=0.1, device=0):
+            dg_steps=STEPS, weight_decay=0.1, err_steps=ERR_STEPS, device=0):
+        """Members on all rows; then max(n_models, 2) networks with the same
+        settings, each without one fold of the rows (row index modulo the
+        fold count), give every row an out-of-fold RMS error, and the error
+        network learns its logarithm."""
+        gpu = _pkg().gpu
         x = features(params)
         y = np.asarray(targets, dtype=np.float64).reshape(len(x), -1)
         mu = y.mean(axis=0)
         sigma = float((y - mu).std())
         t = ((y - mu) / sigma).astype(np.float32)
         rng = np.random.default_rng(seed)
+
+        def train(widths, rows, target, n_steps, lr0, wd):
+            net = gpu.Network(widths, device=device)
+            net.set_params(_init(widths, int(rng.integers(1 << 30))))
+            net.set_data(x[rows], target[rows])
+            loss = net.train(n_steps, batch, lr0, lr_final, seed=int(rng.integers(1 << 62)), weight_decay=wd)
+            return net, loss
+
+        everything = np.arange(len(x))
         plist, losses = [], []
-        for m in range(n_models):
-            net = _pkg().gpu.Network(WIDTHS, device=device)
-            net.set_params(_init(WIDTHS, int(rng.integers(1 << 30))))
-            net.set_data(x, t)
-            losses.append(net.train(steps, batch, lr, lr_final, seed=int(rng.integers(1 << 62)),
-                                    weight_decay=weight_decay))
+        for _ in range(n_models):
+            net, loss = train(WIDTHS, everything, t, steps, lr, weight_decay)
             plist.append(net.get_params())
+            losses.append(loss)
             net.close()
-        s = cls(plist, mu, sigma, grid=grid, steps=dg_steps, device=device)
+        k_folds = max(n_models, 2)
+        fold = everything % k_folds
+        oof = np.zeros_like(y)
+        for k in range(k_folds):
+            net, _ = train(WIDTHS, np.nonzero(fold != k)[0], t, steps, lr, weight_decay)
+            oof[fold == k] = net.forward(x[fold == k]).astype(np.float64) * sigma + mu
+            net.close()
+        le = np.log(np.maximum(rms_db(oof, y), 1e-6))
+        err_mu, err_sigma = float(le.mean()), float(max(le.std(), 1e-6))
+        te = ((le - err_mu) / err_sigma).astype(np.float32).reshape(-1, 1)
+        enet, eloss = train(ERR_WIDTHS, everything, te, err_steps, ERR_LR, ERR_WEIGHT_DECAY)
+        s = cls(plist, mu, sigma, enet.get_params(), err_mu, err_sigma, grid=grid, steps=dg_steps, device=device)
+        enet.close()
         s.train_losses = losses
+        s.err_train_loss = eloss
+        s.oof_rms_db = np.exp(le)
         return s
 
     def predict(self, params):
@@ -208,29 +274,32 @@ class Surrogate:
         x = features(params)
         ys = [net.forward(x).astype(np.float64) * self.sigma + self.mu for net in self.nets]
         mean = np.mean(ys, axis=0)
-        if len(ys) > 1:
-            # spread of the members around their mean (RMS over outputs)
-            est = self.scale * np.sqrt(np.mean([rms_db(y, mean) ** 2 for y in ys], axis=0) * len(ys) / (len(ys) - 1))
-        else:
-            est = np.zeros(len(x))
+        est = np.exp(self.err_net.forward(x)[:, 0].astype(np.float64) * self.err_sigma + self.err_mu)
         return mean.reshape(-1, N_OBS, N_BINS), est
 
-    def calibrate(self, params, targets, coverage=0.95):
-        """Scale the disagreement so that it bounds the true error of the
-        given fraction of these (held-out) queries."""
-        self.scale = 1.0
+    def calibrate(self, params, targets):
+        """Keep the estimates and true errors of these (held-out) queries:
+        they set each bound's acceptance threshold. Returns the median true
+        error."""
         mean, est = self.predict(params)
-        err = rms_db(mean, targets)
-        ratio = err / np.maximum(est, 1e-12)
-        self.scale = float(np.quantile(ratio, coverage))
-        return self.scale
+        self.calib_est = est
+        self.calib_err = rms_db(mean, targets)
+        return float(np.median(self.calib_err))
+
+    def threshold(self, bound_db):
+        """Largest estimated error accepted under bound_db (accept_threshold
+        over the calibration split; -inf before calibration)."""
+        if bound_db == np.inf:
+            return np.inf
+        return accept_threshold(self.calib_est, self.calib_err, bound_db)
 
     def query(self, params, bound_db=1.0, fallback=True):
         """Spectra for parameter rows: the surrogate where its estimated error
-        is within bound_db, the DG runs it was trained on for the rest (when
-        fallback is set). Returns (spectra, from_dg mask, estimated error)."""
+        is within the bound's acceptance threshold, the DG runs it was
+        trained on for the rest (when fallback is set). Returns (spectra,
+        from_dg mask, estimated error)."""
         mean, est = self.predict(params)
-        from_dg = est > bound_db
+        from_dg = est > self.threshold(bound_db)
         if fallback and from_dg.any():
             P = np.asarray(params, dtype=np.float64).reshape(-1, 6)
             mean[from_dg], _ = dg_spectra(P[from_dg], steps=self.steps, grid=self.grid)
@@ -238,30 +307,45 @@ class Surrogate:
 
     def save(self, path):
         """Weights as their BF16 values (what the forward pass uses, so a
-        loaded surrogate answers exactly as this one), biases and the
-        normalisation in FP32."""
+        loaded surrogate answers exactly as this one), biases, the
+        normalisations and the calibration split in FP32/FP64."""
         params = np.stack([n.get_params() for n in self.nets])
         wmask = _weight_mask(WIDTHS)
         w16 = (_bf16_bits(params[:, wmask]) >> 16).astype(np.uint16)
+        ep = self.err_net.get_params()
+        emask = _weight_mask(ERR_WIDTHS)
         np.savez_compressed(path, weights_bf16=w16, biases=params[:, ~wmask], mu=self.mu, sigma=self.sigma,
-                            scale=self.scale, widths=np.array(WIDTHS), grid=self.grid, steps=self.steps)
+                            err_weights_bf16=(_bf16_bits(ep[emask]) >> 16).astype(np.uint16), err_biases=ep[~emask],
+                            err_mu=self.err_mu, err_sigma=self.err_sigma, calib_est=self.calib_est,
+                            calib_err=self.calib_err, widths=np.array(WIDTHS), err_widths=np.array(ERR_WIDTHS),
+                            grid=self.grid, steps=self.steps)
 
     @classmethod
     def load(cls, path, device=0):
         d = np.load(path)
         if list(d["widths"]) != WIDTHS:
             raise ValueError("network widths in %s differ from %s" % (path, WIDTHS))
-        wmask = _weight_mask(WIDTHS)
-        w16, b = d["weights_bf16"], d["biases"]
-        params = np.zeros((w16.shape[0], wmask.size), dtype=np.float32)
-        params[:, wmask] = (w16.astype(np.uint32) << 16).view(np.float32)
-        params[:, ~wmask] = b
-        return cls(list(params), d["mu"], float(d["sigma"]), float(d["scale"]), int(d["grid"]), int(d["steps"]),
-                   device=device)
+        if "err_widths" not in d or list(d["err_widths"]) != ERR_WIDTHS:
+            raise ValueError("%s holds no error network of widths %s" % (path, ERR_WIDTHS))
+
+        def unpack(w16, b, widths):
+            mask = _weight_mask(widths)
+            w16 = np.atleast_2d(w16)
+            p = np.zeros((w16.shape[0], mask.size), dtype=np.float32)
+            p[:, mask] = (w16.astype(np.uint32) << 16).view(np.float32)
+            p[:, ~mask] = np.atleast_2d(b)
+            return p
+
+        params = unpack(d["weights_bf16"], d["biases"], WIDTHS)
+        ep = unpack(d["err_weights_bf16"], d["err_biases"], ERR_WIDTHS)[0]
+        return cls(list(params), d["mu"], float(d["sigma"]), ep, float(d["err_mu"]), float(d["err_sigma"]),
+                   d["calib_est"], d["calib_err"], int(d["grid"]), int(d["steps"]), device=device)
 
     def close(self):
         for n in self.nets:
             n.close()
+        if getattr(self, "err_net", None) is not None:
+            self.err_net.close()
 
 
 def _weight_mask(widths):

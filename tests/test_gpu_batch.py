@@ -97,3 +97,29 @@ def test_batch_fp32_within_1e5_of_fp64(pkg):
     for k, i in enumerate(insts):
         nv = i["mesh"]["dim"] + 1
         assert rel_l2(s32[k][:nv], s64[k][:nv]) <= 1e-5, (k, rel_l2(s32[k][:nv], s64[k][:nv]))
+
+
+def test_sources_covering_no_node(pkg):
+    """A source whose radius holds no node overwrites nothing (as in the
+    reference's node selection): a batch in which every instance of an
+    element type has such a source runs, and each instance matches its
+    single-instance run with the same empty source."""
+    insts = _instances(pkg)[:2]  # 2-D squares of orders 2 and 3: one group each
+    for i in insts:
+        i["src"] = list(i["src"])
+        i["src"][3] = 1e-9
+    nsteps = 10
+    states, obs, _ = _run_batch(pkg, insts, nsteps, pkg.gpu.DG_FP64)
+    for k, i in enumerate(insts):
+        sd, od, ow = _sets(i["mesh"], i["src"], i["obs"])
+        assert sd[0].size == 0
+        S = pkg.gpu.Solver(i["mesh"], v0=i["v0"], rho0=1.225, c0=100.0, precision=pkg.gpu.DG_FP64)
+        S.set_state(smooth_state(i["mesh"], seed=i["seed"]))
+        S.set_sources(sd)
+        S.set_source_values(_values(i, nsteps))
+        S.set_observers(od, ow)
+        _, o = S.run(nsteps, i["dt"])
+        u = S.get_state()
+        S.close()
+        assert rel_l2(states[k][:3], u[:3]) <= 1e-13, k
+        assert rel_l2(obs[k], o) <= 1e-13, k

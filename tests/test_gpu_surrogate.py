@@ -5,8 +5,9 @@ training runs) so that DG data generation and training take seconds.
 What the network gains: it answers queries at >= 100x the rate of the DG
 runs it replaces (timed at the shipped DG configuration), it predicts
 held-out spectra better than the best constant guess (the mean training
-spectrum), and its fallback hands every query whose estimated error is above
-the bound back to DG, whose answers it returns unchanged."""
+spectrum), its error network's estimate follows the true error, and its
+fallback hands every query whose estimate is above the bound's acceptance
+threshold back to DG, whose answers it returns unchanged."""
 import time
 
 import numpy as np
@@ -46,7 +47,19 @@ def test_surrogate_beats_constant_guess(trained):
     err = S.rms_db(mean, Y_test)
     base = S.rms_db(np.broadcast_to(Y_train[:500].mean(axis=0), Y_test.shape), Y_test)
     assert np.median(err) < 0.7 * np.median(base), (np.median(err), np.median(base))
-    assert np.all(est >= 0)
+    assert np.all(est > 0)
+
+
+def test_error_estimate_follows_true_error(trained):
+    """The error network ranks held-out queries by their true error better
+    than chance (rank correlation), and the out-of-fold errors it learned
+    from are of the size of the held-out errors."""
+    S, sur, _, _, P_test, Y_test, _ = trained
+    mean, est = sur.predict(P_test)
+    err = S.rms_db(mean, Y_test)
+    r = np.corrcoef(np.argsort(np.argsort(est)), np.argsort(np.argsort(err)))[0, 1]
+    assert r > 0.2, r
+    assert 0.5 < np.median(sur.oof_rms_db) / np.median(err) < 2.0
 
 
 def test_surrogate_throughput_over_dg(trained):
@@ -83,9 +96,11 @@ def test_fallback_returns_dg_answers(trained):
     np.testing.assert_array_equal(spec2, mean)
     # a mixed bound: accepted rows come from the network, the others from DG
     _, est = sur.predict(q)
-    b = float(np.median(est))
+    t = float(np.median(est))
+    # the loosest bound whose acceptance threshold is below t
+    b = max((x for x in np.sort(sur.calib_err) if sur.threshold(x) < t), default=-1.0)
     spec3, from_dg3, _ = sur.query(q, bound_db=b)
-    assert np.array_equal(from_dg3, est > b)
+    assert np.array_equal(from_dg3, est > sur.threshold(b))
     np.testing.assert_allclose(spec3[from_dg3], Y_test[:12][from_dg3], rtol=0, atol=1e-3)
     np.testing.assert_array_equal(spec3[~from_dg3], mean[~from_dg3])
 
