@@ -575,17 +575,28 @@ int select_variant(dg_ctx* c, int want) {
   }
   float best = 1e30f;
   int best_v = -1;
-  for (int v : cands) {
-    if (!set_variant(c, v)) continue;
-    // stages 1-3 of an RK step (their operand mixes differ; stage 4 would
-    // write the state), once to warm up, then three times timed
+  // the four stages of an RK step (their operand mixes differ); stage 4
+  // updates a stage buffer in place of the state, which stays untouched
+  auto rk_stages = [&]() {
     cudaError_t err = cudaSuccess;
     for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
+    if (err == cudaSuccess) {
+      void* u = c->u;
+      c->u = c->y1;
+      err = launch_stage(c, 4, c->y0, nullptr, nullptr, 1e-30);
+      c->u = u;
+    }
+    return err;
+  };
+  for (int v : cands) {
+    if (!set_variant(c, v)) continue;
+    // once to warm up, then three times timed
+    cudaError_t err = rk_stages();
     float tot = 0.f;
     for (int r = 0; r < 3 && err == cudaSuccess; ++r) {
       if (flush) k_flush<<<2 * c->num_sms, 512, 0, c->stream>>>(flush, flush_words, (unsigned)r);
       cudaEventRecord(e0, c->stream);
-      for (int st = 1; st <= 3 && err == cudaSuccess; ++st) err = launch_stage(c, st, c->y0, c->y1, nullptr, 1e-30);
+      err = rk_stages();
       cudaEventRecord(e1, c->stream);
       if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
       float ms = 0.f;
@@ -604,7 +615,8 @@ int select_variant(dg_ctx* c, int want) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
-  // the timing runs wrote the accumulator and stage buffers only; clear them
+  // the timing runs wrote the accumulator, the stage buffers and the
+  // residual partial sums only; clear the buffers
   const size_t nb = (size_t)c->nv * c->Epad * c->np * c->tsize;
   cudaMemsetAsync(c->acc, 0, nb, c->stream);
   cudaMemsetAsync(c->y0, 0, nb, c->stream);

@@ -19,6 +19,7 @@
 // and finishes its loop without further waiting.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 #include "dg_internal.cuh"
 
@@ -386,19 +387,54 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
 #pragma unroll
         for (int q = 0; q < NV; ++q) W[r][ii][q] = 0;
     const T* ye = sY + e * NP;
+    if constexpr (std::is_same<T, float>::value && NC % 2 == 0) {
+      // FP32 with an even node count per thread: the node pairs' FMAs as
+      // packed pairs (per component the rounding of fmaf, the same result)
+      float2 W2[D][NC / 2][NV];
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int h = 0; h < NC / 2; ++h)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) W2[r][h][q] = make_float2(0.f, 0.f);
 #pragma unroll 4
-    for (int j = 0; j < NP; ++j) {
-      T yq[NV];
+      for (int j = 0; j < NP; ++j) {
+        float yq[NV];
 #pragma unroll
-      for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
+        for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
 #pragma unroll
-      for (int r = 0; r < D; ++r) {
-        T dv[NC];
-        load_chunk<T, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
+        for (int r = 0; r < D; ++r) {
+          float dv[NC];
+          load_chunk<float, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
 #pragma unroll
-        for (int ii = 0; ii < NC; ++ii)
+          for (int h = 0; h < NC / 2; ++h) {
+            const float2 dp = make_float2(dv[2 * h], dv[2 * h + 1]);
 #pragma unroll
-          for (int q = 0; q < NV; ++q) W[r][ii][q] += dv[ii] * yq[q];
+            for (int q = 0; q < NV; ++q) W2[r][h][q] = __ffma2_rn(dp, make_float2(yq[q], yq[q]), W2[r][h][q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int h = 0; h < NC / 2; ++h)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) W[r][2 * h][q] = W2[r][h][q].x, W[r][2 * h + 1][q] = W2[r][h][q].y;
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < NP; ++j) {
+        T yq[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) yq[q] = ye[q * ET * NP + j];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          T dv[NC];
+          load_chunk<T, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
+#pragma unroll
+          for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) W[r][ii][q] += dv[ii] * yq[q];
+        }
       }
     }
     const T* G = sGF + e * RECF;
