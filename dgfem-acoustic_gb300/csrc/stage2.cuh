@@ -355,7 +355,8 @@ struct Pipe {
 // gathers, volume term, face fluxes, lift and the RK update. The tile's stage
 // input and geometry records (sY, sGF, sGI) have arrived; its RK operands sE
 // (u, accumulator, snapshot: nepi of them) arrive on bar_epi with phase parity
-// epi_parity. The caller synchronises the block before the buffers are reused.
+// epi_parity. sD holds Dt, sL the negated LIFT table. The caller
+// synchronises the block before the buffers are reused.
 template <class C, typename T>
 __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* sY, const T* sGF, const int* sGI,
                                           const T* sE, T* sN, const T* sD, const T* sL, const short* sFm,
@@ -387,16 +388,20 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
 #pragma unroll
         for (int q = 0; q < NV; ++q) W[r][ii][q] = 0;
     const T* ye = sY + e * NP;
-    if constexpr (std::is_same<T, float>::value && NC % 2 == 0) {
-      // FP32 with an even node count per thread: the node pairs' FMAs as
-      // packed pairs (per component the rounding of fmaf, the same result)
-      float2 W2[D][NC / 2][NV];
+    if constexpr (std::is_same<T, float>::value && NC >= 2) {
+      // FP32: the FMAs of node pairs as packed pairs (per component the
+      // rounding of fmaf, the same result); an odd last node stays scalar
+      constexpr int NH = NC / 2;
+      float2 W2[D][NH][NV];
+      float W1[D][NV];
 #pragma unroll
       for (int r = 0; r < D; ++r)
 #pragma unroll
-        for (int h = 0; h < NC / 2; ++h)
+        for (int q = 0; q < NV; ++q) {
+          W1[r][q] = 0.f;
 #pragma unroll
-          for (int q = 0; q < NV; ++q) W2[r][h][q] = make_float2(0.f, 0.f);
+          for (int h = 0; h < NH; ++h) W2[r][h][q] = make_float2(0.f, 0.f);
+        }
 #pragma unroll 4
       for (int j = 0; j < NP; ++j) {
         float yq[NV];
@@ -407,19 +412,25 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
           float dv[NC];
           load_chunk<float, NC, C::VW, NP>(dv, sD + (r * NP + j) * NP, i0);
 #pragma unroll
-          for (int h = 0; h < NC / 2; ++h) {
+          for (int h = 0; h < NH; ++h) {
             const float2 dp = make_float2(dv[2 * h], dv[2 * h + 1]);
 #pragma unroll
             for (int q = 0; q < NV; ++q) W2[r][h][q] = __ffma2_rn(dp, make_float2(yq[q], yq[q]), W2[r][h][q]);
+          }
+          if constexpr (NC % 2 != 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) W1[r][q] += dv[NC - 1] * yq[q];
           }
         }
       }
 #pragma unroll
       for (int r = 0; r < D; ++r)
 #pragma unroll
-        for (int h = 0; h < NC / 2; ++h)
+        for (int q = 0; q < NV; ++q) {
 #pragma unroll
-          for (int q = 0; q < NV; ++q) W[r][2 * h][q] = W2[r][h][q].x, W[r][2 * h + 1][q] = W2[r][h][q].y;
+          for (int h = 0; h < NH; ++h) W[r][2 * h][q] = W2[r][h][q].x, W[r][2 * h + 1][q] = W2[r][h][q].y;
+          if constexpr (NC % 2 != 0) W[r][NC - 1][q] = W1[r][q];
+        }
     } else {
 #pragma unroll 4
       for (int j = 0; j < NP; ++j) {
@@ -477,19 +488,49 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
   if (active) face_fluxes<C, T>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
   __syncthreads();
 
-  // ---- lifting ----
+  // ---- lifting (sL holds -LIFT: the products accumulate) ----
   if (active) {
     const T* hrow = sN + (size_t)e * C::SN_EL;
+    if constexpr (std::is_same<T, float>::value && NC >= 2) {
+      constexpr int NH = NC / 2;
+      float2 L2[NH][NV];
+#pragma unroll
+      for (int h = 0; h < NH; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) L2[h][q] = make_float2(Lv[2 * h][q], Lv[2 * h + 1][q]);
 #pragma unroll 4
-    for (int k = 0; k < NK; ++k) {
-      T hq[C::NVQ];
-      vload<T, C::NVQ>(hq, hrow + k * C::NVQ);
-      T lv[NC];
-      load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
+      for (int k = 0; k < NK; ++k) {
+        float hq[C::NVQ];
+        vload<float, C::NVQ>(hq, hrow + k * C::NVQ);
+        float lv[NC];
+        load_chunk<float, NC, C::VW, NP>(lv, sL + k * NP, i0);
 #pragma unroll
-      for (int ii = 0; ii < NC; ++ii)
+        for (int h = 0; h < NH; ++h) {
+          const float2 lp = make_float2(lv[2 * h], lv[2 * h + 1]);
 #pragma unroll
-        for (int q = 0; q < NV; ++q) Lv[ii][q] -= lv[ii] * hq[q];
+          for (int q = 0; q < NV; ++q) L2[h][q] = __ffma2_rn(lp, make_float2(hq[q], hq[q]), L2[h][q]);
+        }
+        if constexpr (NC % 2 != 0) {
+#pragma unroll
+          for (int q = 0; q < NV; ++q) Lv[NC - 1][q] += lv[NC - 1] * hq[q];
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < NH; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) Lv[2 * h][q] = L2[h][q].x, Lv[2 * h + 1][q] = L2[h][q].y;
+    } else {
+#pragma unroll 4
+      for (int k = 0; k < NK; ++k) {
+        T hq[C::NVQ];
+        vload<T, C::NVQ>(hq, hrow + k * C::NVQ);
+        T lv[NC];
+        load_chunk<T, NC, C::VW, NP>(lv, sL + k * NP, i0);
+#pragma unroll
+        for (int ii = 0; ii < NC; ++ii)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) Lv[ii][q] += lv[ii] * hq[q];
+      }
     }
   }
 
@@ -610,7 +651,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     fence_mbar_init();
   }
   for (int i = tid; i < D * NP * NP; i += NT) sD[i] = a.Dt[i];
-  for (int i = tid; i < NK * NP; i += NT) sL[i] = a.LIFT[i];
+  for (int i = tid; i < NK * NP; i += NT) sL[i] = -a.LIFT[i];  // negated for pipe_tile's lift
   for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
   for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
   __syncthreads();

@@ -102,7 +102,7 @@ struct OpsSm {
     short* sFm = reinterpret_cast<short*>(base + (C::oFm - C::oD));
     short* sNb = reinterpret_cast<short*>(base + (C::oNb - C::oD));
     for (int i = tid; i < D * NP * NP; i += kMultiNT) sD[i] = a.Dt[i];
-    for (int i = tid; i < NK * NP; i += kMultiNT) sL[i] = a.LIFT[i];
+    for (int i = tid; i < NK * NP; i += kMultiNT) sL[i] = -a.LIFT[i];  // negated for pipe_tile's lift
     for (int i = tid; i < NK; i += kMultiNT) sFm[i] = a.fmask[i];
     for (int i = tid; i < NF * NPERM * NFP; i += kMultiNT) sNb[i] = a.nbrnode[i];
   }
