@@ -288,8 +288,15 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
           for (int q = 0; q < NV; ++q) up[q] = yn[q * ET * NP + nn];
         } else {
           const T* slot = srow + m * C::SN_K;
+          if constexpr (C::SN_Q == 1) {
+            T hv[C::NVQ];  // the node's gathered variables in one vector load
+            vload<T, C::NVQ>(hv, slot);
 #pragma unroll
-          for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * C::SN_Q];
+            for (int q = 0; q < NV; ++q) up[q] = hv[q];
+          } else {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) up[q] = slot[(size_t)q * C::SN_Q];
+          }
         }
         T avg[NV], dif[NV];
 #pragma unroll
