@@ -267,8 +267,8 @@ int dg_batch_fused(const dg_batch* b);
 
 /* ------------------------------------------------------------------------
  * Learned spectral surrogate (no counterpart in the reference, which answers
- * every parameter query with a DG run; DG stays the fallback and the judge
- * of the surrogate's error). A fully connected network: widths[0] inputs,
+ * every parameter query with a DG run; DG stays the fallback and the
+ * measure of the surrogate's error). A fully connected network: widths[0] inputs,
  * n_layers - 1 GELU hidden layers, a linear output layer of widths[n_layers];
  * BF16 weights in the forward/backward passes, FP32 master weights, FP32
  * accumulation. Parameters are one flat FP32 vector, layer after layer:
