@@ -68,18 +68,21 @@ __global__ void k_inject(T* up, const int64_t* dof, const int* off, const int* i
   if (any) up[dof[i]] = (T)v;
 }
 
-constexpr int kFinalizeThreads = 256;
+// Block sizes of the finalize kernel: 256 threads when an observer holds
+// more node slots than the small block (one slot per thread), else 64.
+constexpr int kFinalizeThreads = 256, kFinalizeThreadsSmall = 64;
 
 // Block sums of five FP64 values per thread by a halving tree in shared
 // memory, each level with only the warps it needs (GB300's FP64 rate makes
 // per-warp shuffle trees, which add on every lane at every level, the larger
 // cost). The sums end in red[c][0]; every thread of the block calls it.
-__device__ __forceinline__ void block_sum5(double (&red)[5][kFinalizeThreads], const double (&acc)[5], int tid) {
+template <int NT>
+__device__ __forceinline__ void block_sum5(double (&red)[5][NT], const double (&acc)[5], int tid) {
 #pragma unroll
   for (int c = 0; c < 5; ++c) red[c][tid] = acc[c];
   __syncthreads();
 #pragma unroll
-  for (int s = kFinalizeThreads / 2; s > 0; s >>= 1) {
+  for (int s = NT / 2; s > 0; s >>= 1) {
     if (tid < s) {
 #pragma unroll
       for (int c = 0; c < 5; ++c) red[c][tid] += red[c][tid + s];
@@ -91,24 +94,24 @@ __device__ __forceinline__ void block_sum5(double (&red)[5][kFinalizeThreads], c
 // Residuals (block 0) and observer IDW samples (then obs_blocks blocks per
 // observer, each summing a strided share of its node slots) of the step just
 // completed (src/solver.cpp:518-573). With more than one block per
-// observer, the blocks store partial sums and the last block to finish
-// (counted with an atomic) combines them in block order: the result does not
-// depend on the blocks' timing.
-template <typename T>
-__global__ void __launch_bounds__(kFinalizeThreads)
+// observer, the blocks store partial sums and the observer's last block to
+// finish (counted with an atomic per observer) combines them in block order:
+// the result does not depend on the blocks' timing.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT)
     k_finalize(const double* partials, int nparts, double inv_count, double* res, const T* u, int64_t stride, int nv,
                const int64_t* odof, const int64_t* ooff, const double* ow, double* obs, int n_obs, int obs_blocks,
                double* obs_part, unsigned* obs_cnt, const int64_t* step, int64_t cap) {
-  __shared__ double red[5][kFinalizeThreads];
+  __shared__ double red[5][NT];
   __shared__ bool last;
   int64_t slot = step[0] - step[1];
   if (slot < 0 || slot >= cap) return;
   const int tid = threadIdx.x;
   if (blockIdx.x == 0) {
     double acc[5] = {0, 0, 0, 0, 0};
-    for (int b = tid; b < nparts; b += kFinalizeThreads)
+    for (int b = tid; b < nparts; b += NT)
       for (int c = 0; c < 5; ++c) acc[c] += partials[b * 5 + c];
-    block_sum5(red, acc, tid);
+    block_sum5<NT>(red, acc, tid);
     if (tid < 5) res[slot * 5 + tid] = red[tid][0] * inv_count;
     return;
   }
@@ -116,9 +119,9 @@ __global__ void __launch_bounds__(kFinalizeThreads)
   const int o = ob / obs_blocks, part = ob - o * obs_blocks;
   if (o >= n_obs) return;
   double acc[5] = {0, 0, 0, 0, 0};  // p, vx, vy, vz, w
-  const int64_t step_k = (int64_t)kFinalizeThreads * obs_blocks;
+  const int64_t step_k = (int64_t)NT * obs_blocks;
 #pragma unroll 4
-  for (int64_t k = ooff[o] + (int64_t)part * kFinalizeThreads + tid; k < ooff[o + 1]; k += step_k) {
+  for (int64_t k = ooff[o] + (int64_t)part * NT + tid; k < ooff[o + 1]; k += step_k) {
     double w = ow[k];
     int64_t d = odof[k];
 #pragma unroll
@@ -126,7 +129,7 @@ __global__ void __launch_bounds__(kFinalizeThreads)
       if (q < nv) acc[q] += (double)u[q * stride + d] * w;
     acc[4] += w;
   }
-  block_sum5(red, acc, tid);
+  block_sum5<NT>(red, acc, tid);
   if (obs_blocks == 1) {
     if (tid < 4) obs[(slot * n_obs + o) * 4 + tid] = red[tid][0] / red[4][0];
     return;
@@ -136,23 +139,36 @@ __global__ void __launch_bounds__(kFinalizeThreads)
     __threadfence();
   }
   __syncthreads();
-  if (tid == 0) last = atomicAdd(obs_cnt, 1u) == (unsigned)(n_obs * obs_blocks - 1);
+  if (tid == 0) last = atomicAdd(obs_cnt + o, 1u) == (unsigned)(obs_blocks - 1);
   __syncthreads();
   if (!last) return;
   __threadfence();
-  for (int i = tid; i < n_obs * 4; i += kFinalizeThreads) {
-    const int oo = i >> 2, q = i & 3;
+  if (tid < 4) {
     double v = 0.0, w = 0.0;
     for (int b = 0; b < obs_blocks; ++b) {
-      v += __ldcg(obs_part + ((int64_t)oo * obs_blocks + b) * 5 + q);
-      w += __ldcg(obs_part + ((int64_t)oo * obs_blocks + b) * 5 + 4);
+      v += __ldcg(obs_part + ((int64_t)o * obs_blocks + b) * 5 + tid);
+      w += __ldcg(obs_part + ((int64_t)o * obs_blocks + b) * 5 + 4);
     }
-    obs[(slot * n_obs + oo) * 4 + q] = v / w;
+    obs[(slot * n_obs + o) * 4 + tid] = v / w;
   }
-  if (tid == 0) *obs_cnt = 0u;  // for the next step
+  if (tid == 0) obs_cnt[o] = 0u;  // for the next step
 }
 
 __global__ void k_advance(int64_t* step) { step[0] += 1; }
+
+template <typename T, int NT>
+void launch_finalize_nt(dg_ctx* c, int nparts, double inv_count, int64_t stride) {
+  k_finalize<T, NT><<<1 + c->n_obs * c->obs_blocks, NT, 0, c->stream>>>(
+      c->partials, nparts, inv_count, c->d_res, (const T*)c->u, stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w,
+      c->d_obs, c->n_obs, c->obs_blocks, c->d_obs_part, c->d_obs_cnt, c->d_step, c->out_cap);
+}
+template <typename T>
+void launch_finalize(dg_ctx* c, int nparts, double inv_count, int64_t stride) {
+  if (c->obs_small)
+    launch_finalize_nt<T, kFinalizeThreadsSmall>(c, nparts, inv_count, stride);
+  else
+    launch_finalize_nt<T, kFinalizeThreads>(c, nparts, inv_count, stride);
+}
 
 // Euler1 commit: u = y (computed as u + k by the stage kernel) with residuals.
 template <typename T>
@@ -314,16 +330,10 @@ cudaError_t enqueue_finalize(dg_ctx* c, int nparts) {
   double inv_count = 1.0 / (double)(c->E * c->np);
   // an observer with thousands of node slots is summed by several blocks:
   // the sums are FP64, whose rate per SM on GB300 bounds a single block
-  const int nblk = 1 + c->n_obs * c->obs_blocks;
   if (c->prec == DG_FP32)
-    k_finalize<float><<<nblk, kFinalizeThreads, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res, (const float*)c->u, stride,
-                                                    c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w, c->d_obs, c->n_obs,
-                                                    c->obs_blocks, c->d_obs_part, c->d_obs_cnt, c->d_step, c->out_cap);
+    launch_finalize<float>(c, nparts, inv_count, stride);
   else
-    k_finalize<double><<<nblk, kFinalizeThreads, 0, c->stream>>>(c->partials, nparts, inv_count, c->d_res, (const double*)c->u,
-                                                     stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w, c->d_obs,
-                                                     c->n_obs, c->obs_blocks, c->d_obs_part, c->d_obs_cnt, c->d_step,
-                                                     c->out_cap);
+    launch_finalize<double>(c, nparts, inv_count, stride);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_advance<<<1, 1, 0, c->stream>>>(c->d_step);
@@ -1045,6 +1055,7 @@ int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t
   c->d_obs_dof = nullptr, c->d_obs_off = nullptr, c->d_obs_w = nullptr, c->d_obs_part = nullptr;
   c->d_obs_cnt = nullptr;
   c->obs_blocks = 1;
+  c->obs_small = true;
   c->n_obs = n_obs;
   if (c->d_obs) cudaFree(c->d_obs), c->d_obs = nullptr;
   if (c->d_res) cudaFree(c->d_res), c->d_res = nullptr;
@@ -1074,11 +1085,12 @@ int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t
   // blocks per observer: one node slot per thread, at most 64 blocks
   int64_t most = 0;
   for (int o = 0; o < n_obs; ++o) most = std::max<int64_t>(most, offsets[o + 1] - offsets[o]);
+  c->obs_small = most <= kFinalizeThreadsSmall;
   const int ob = (int)std::min<int64_t>(64, std::max<int64_t>(1, (most + kFinalizeThreads - 1) / kFinalizeThreads));
   if (ob > 1) {
     CK(c, cudaMalloc(&c->d_obs_part, (size_t)n_obs * ob * 5 * sizeof(double)));
-    CK(c, cudaMalloc(&c->d_obs_cnt, sizeof(unsigned)));
-    CK(c, cudaMemsetAsync(c->d_obs_cnt, 0, sizeof(unsigned), c->stream));
+    CK(c, cudaMalloc(&c->d_obs_cnt, (size_t)n_obs * sizeof(unsigned)));
+    CK(c, cudaMemsetAsync(c->d_obs_cnt, 0, (size_t)n_obs * sizeof(unsigned), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     c->obs_blocks = ob;
   }

@@ -65,9 +65,10 @@ struct dg_ctx {
   int64_t* d_obs_off = nullptr;
   double* d_obs_w = nullptr;
   // observers with many node slots are summed by obs_blocks blocks each:
-  // per-block partial sums [n_obs][obs_blocks][5] and the count of blocks
-  // done (the last one combines them in block order)
+  // per-block partial sums [n_obs][obs_blocks][5] and per observer the count
+  // of its blocks done (the last one combines them in block order)
   int obs_blocks = 1;
+  bool obs_small = true;  // every observer within the small finalize block
   double* d_obs_part = nullptr;
   unsigned* d_obs_cnt = nullptr;
   // curved elements (curved.cu): slot table, per-element quadrature data and
