@@ -91,17 +91,19 @@ __device__ __forceinline__ void block_sum5(double (&red)[5][NT], const double (&
   }
 }
 
-// Residuals (block 0) and observer IDW samples (then obs_blocks blocks per
-// observer, each summing a strided share of its node slots) of the step just
-// completed (src/solver.cpp:518-573). With more than one block per
-// observer, the blocks store partial sums and the observer's last block to
-// finish (counted with an atomic per observer) combines them in block order:
-// the result does not depend on the blocks' timing.
+// Residuals (block 0) and observer IDW samples (then, per observer o, the
+// blocks bfirst[o] .. bfirst[o+1]-1 of the observer blocks, bmap giving each
+// block's observer; each block sums a strided share of the observer's node
+// slots) of the step just completed (src/solver.cpp:518-573). With more than
+// one block per observer, the blocks store partial sums and the observer's
+// last block to finish (counted with an atomic per observer) combines them in
+// block order: the result does not depend on the blocks' timing. Without
+// bmap every observer has one block.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT)
     k_finalize(const double* partials, int nparts, double inv_count, double* res, const T* u, int64_t stride, int nv,
-               const int64_t* odof, const int64_t* ooff, const double* ow, double* obs, int n_obs, int obs_blocks,
-               double* obs_part, unsigned* obs_cnt, const int64_t* step, int64_t cap) {
+               const int64_t* odof, const int64_t* ooff, const double* ow, double* obs, int n_obs, const int* bmap,
+               const int* bfirst, double* obs_part, unsigned* obs_cnt, const int64_t* step, int64_t cap) {
   __shared__ double red[5][NT];
   __shared__ bool last;
   int64_t slot = step[0] - step[1];
@@ -116,10 +118,11 @@ __global__ void __launch_bounds__(NT)
     return;
   }
   const int ob = blockIdx.x - 1;
-  const int o = ob / obs_blocks, part = ob - o * obs_blocks;
+  const int o = bmap ? bmap[ob] : ob;
   if (o >= n_obs) return;
+  const int first = bmap ? bfirst[o] : ob, nb = bmap ? bfirst[o + 1] - first : 1, part = ob - first;
   double acc[5] = {0, 0, 0, 0, 0};  // p, vx, vy, vz, w
-  const int64_t step_k = (int64_t)NT * obs_blocks;
+  const int64_t step_k = (int64_t)NT * nb;
 #pragma unroll 4
   for (int64_t k = ooff[o] + (int64_t)part * NT + tid; k < ooff[o + 1]; k += step_k) {
     double w = ow[k];
@@ -130,7 +133,7 @@ __global__ void __launch_bounds__(NT)
     acc[4] += w;
   }
   block_sum5<NT>(red, acc, tid);
-  if (obs_blocks == 1) {
+  if (nb == 1) {
     if (tid < 4) obs[(slot * n_obs + o) * 4 + tid] = red[tid][0] / red[4][0];
     return;
   }
@@ -139,15 +142,15 @@ __global__ void __launch_bounds__(NT)
     __threadfence();
   }
   __syncthreads();
-  if (tid == 0) last = atomicAdd(obs_cnt + o, 1u) == (unsigned)(obs_blocks - 1);
+  if (tid == 0) last = atomicAdd(obs_cnt + o, 1u) == (unsigned)(nb - 1);
   __syncthreads();
   if (!last) return;
   __threadfence();
   if (tid < 4) {
     double v = 0.0, w = 0.0;
-    for (int b = 0; b < obs_blocks; ++b) {
-      v += __ldcg(obs_part + ((int64_t)o * obs_blocks + b) * 5 + tid);
-      w += __ldcg(obs_part + ((int64_t)o * obs_blocks + b) * 5 + 4);
+    for (int b = first; b < first + nb; ++b) {
+      v += __ldcg(obs_part + (int64_t)b * 5 + tid);
+      w += __ldcg(obs_part + (int64_t)b * 5 + 4);
     }
     obs[(slot * n_obs + o) * 4 + tid] = v / w;
   }
@@ -158,9 +161,9 @@ __global__ void k_advance(int64_t* step) { step[0] += 1; }
 
 template <typename T, int NT>
 void launch_finalize_nt(dg_ctx* c, int nparts, double inv_count, int64_t stride) {
-  k_finalize<T, NT><<<1 + c->n_obs * c->obs_blocks, NT, 0, c->stream>>>(
+  k_finalize<T, NT><<<1 + c->obs_blocks, NT, 0, c->stream>>>(
       c->partials, nparts, inv_count, c->d_res, (const T*)c->u, stride, c->nv, c->d_obs_dof, c->d_obs_off, c->d_obs_w,
-      c->d_obs, c->n_obs, c->obs_blocks, c->d_obs_part, c->d_obs_cnt, c->d_step, c->out_cap);
+      c->d_obs, c->n_obs, c->d_obs_bmap, c->d_obs_bfirst, c->d_obs_part, c->d_obs_cnt, c->d_step, c->out_cap);
 }
 template <typename T>
 void launch_finalize(dg_ctx* c, int nparts, double inv_count, int64_t stride) {
@@ -939,7 +942,8 @@ int dg_destroy(dg_ctx* c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (void* p : c->allocs) cudaFree(p);
   void* extra[] = {c->d_res, c->d_obs, c->d_src_dof, c->d_src_off, c->d_src_ids, c->d_srcval,
-                   c->d_obs_dof, c->d_obs_off, c->d_obs_w, c->d_obs_part, c->d_obs_cnt};
+                   c->d_obs_dof, c->d_obs_off, c->d_obs_w, c->d_obs_part, c->d_obs_cnt, c->d_obs_bmap,
+                   c->d_obs_bfirst};
   for (void* p : extra)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -1050,11 +1054,11 @@ int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t
   if (n_obs > 0 && offsets[n_obs] > 0 && (!dofs || !weights))
     return fail(c, DG_ERR_ARG, "dg_set_observers: dofs or weights is null");
   for (void* p : {(void*)c->d_obs_dof, (void*)c->d_obs_off, (void*)c->d_obs_w, (void*)c->d_obs_part,
-                  (void*)c->d_obs_cnt})
+                  (void*)c->d_obs_cnt, (void*)c->d_obs_bmap, (void*)c->d_obs_bfirst})
     if (p) cudaFree(p);
   c->d_obs_dof = nullptr, c->d_obs_off = nullptr, c->d_obs_w = nullptr, c->d_obs_part = nullptr;
-  c->d_obs_cnt = nullptr;
-  c->obs_blocks = 1;
+  c->d_obs_cnt = nullptr, c->d_obs_bmap = nullptr, c->d_obs_bfirst = nullptr;
+  c->obs_blocks = n_obs;
   c->obs_small = true;
   c->n_obs = n_obs;
   if (c->d_obs) cudaFree(c->d_obs), c->d_obs = nullptr;
@@ -1082,17 +1086,29 @@ int dg_set_observers(dg_ctx* c, int n_obs, const int64_t* offsets, const int64_t
     CK(c, cudaMemcpyAsync(c->d_obs_w, weights, total * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
   }
-  // blocks per observer: one node slot per thread, at most 64 blocks
+  // blocks per observer: one node slot per thread, at most 64 blocks each
   int64_t most = 0;
   for (int o = 0; o < n_obs; ++o) most = std::max<int64_t>(most, offsets[o + 1] - offsets[o]);
   c->obs_small = most <= kFinalizeThreadsSmall;
-  const int ob = (int)std::min<int64_t>(64, std::max<int64_t>(1, (most + kFinalizeThreads - 1) / kFinalizeThreads));
-  if (ob > 1) {
-    CK(c, cudaMalloc(&c->d_obs_part, (size_t)n_obs * ob * 5 * sizeof(double)));
+  if (most > kFinalizeThreads) {
+    std::vector<int> bfirst(n_obs + 1, 0), bmap;
+    for (int o = 0; o < n_obs; ++o) {
+      const int64_t n = offsets[o + 1] - offsets[o];
+      const int b = (int)std::min<int64_t>(64, std::max<int64_t>(1, (n + kFinalizeThreads - 1) / kFinalizeThreads));
+      bfirst[o + 1] = bfirst[o] + b;
+      for (int k = 0; k < b; ++k) bmap.push_back(o);
+    }
+    const int nb = bfirst[n_obs];
+    CK(c, cudaMalloc(&c->d_obs_part, (size_t)nb * 5 * sizeof(double)));
     CK(c, cudaMalloc(&c->d_obs_cnt, (size_t)n_obs * sizeof(unsigned)));
+    CK(c, cudaMalloc(&c->d_obs_bmap, (size_t)nb * sizeof(int)));
+    CK(c, cudaMalloc(&c->d_obs_bfirst, (size_t)(n_obs + 1) * sizeof(int)));
     CK(c, cudaMemsetAsync(c->d_obs_cnt, 0, (size_t)n_obs * sizeof(unsigned), c->stream));
+    CK(c, cudaMemcpyAsync(c->d_obs_bmap, bmap.data(), (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->d_obs_bfirst, bfirst.data(), (size_t)(n_obs + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                          c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    c->obs_blocks = ob;
+    c->obs_blocks = nb;
   }
   return DG_OK;
 }

@@ -64,10 +64,14 @@ struct dg_ctx {
   int64_t* d_obs_dof = nullptr;
   int64_t* d_obs_off = nullptr;
   double* d_obs_w = nullptr;
-  // observers with many node slots are summed by obs_blocks blocks each:
-  // per-block partial sums [n_obs][obs_blocks][5] and per observer the count
+  // observer blocks of the finalize kernel (obs_blocks in all); when an
+  // observer has more node slots than a block has threads, blocks
+  // bfirst[o] .. bfirst[o+1]-1 sum observer o (bmap: block -> observer),
+  // with per-block partial sums [obs_blocks][5] and per observer the count
   // of its blocks done (the last one combines them in block order)
-  int obs_blocks = 1;
+  int obs_blocks = 0;
+  int* d_obs_bmap = nullptr;
+  int* d_obs_bfirst = nullptr;
   bool obs_small = true;  // every observer within the small finalize block
   double* d_obs_part = nullptr;
   unsigned* d_obs_cnt = nullptr;
