@@ -100,6 +100,13 @@ struct ResAcc<float> {
   }
 };
 
+// The RK4 combine's division by 6 (src/solver.cpp:509-516): FP64 divides,
+// as the reference does; FP32 multiplies by the FP32 reciprocal (within an
+// ulp of the division, without the division's instruction sequence, which
+// made the last stage the slowest).
+__device__ __forceinline__ double rk4_sixth(double x) { return x / 6.0; }
+__device__ __forceinline__ float rk4_sixth(float x) { return x * (1.0f / 6.0f); }
+
 // Physical constants used by the kernels.
 struct Phys {
   double v0[3];

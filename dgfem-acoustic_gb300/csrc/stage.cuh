@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(ShapeT<D, P, T>::NT) stage_kernel(const StageA
             a.y_out[g] = a.u[g] + kv;
             break;
           case 4: {
-            const T un = a.u[g] + (a.acc[g] + kv) / (T)6;
+            const T un = a.u[g] + rk4_sixth(a.acc[g] + kv);
             a.u[g] = un;
             racc.add(q, a.snap[g], un, a.c0sq);
             break;

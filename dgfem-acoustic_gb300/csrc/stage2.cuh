@@ -589,7 +589,7 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
           vload<T, VW>(xs, es + lidx);
 #pragma unroll
           for (int v = 0; v < VW; ++v) {
-            const T un = xu[v] + (xa[v] + kv[v]) / (T)6;
+            const T un = xu[v] + rk4_sixth(xa[v] + kv[v]);
             o1[v] = un;
             racc.add(q, xs[v], un, a.c0sq);
           }

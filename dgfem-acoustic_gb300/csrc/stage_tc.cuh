@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
             load4<NP, VW>(x1, r1, i0);
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-              o0[u] = x0[u] + (x1[u] + kv[u]) / (T)6;
+              o0[u] = x0[u] + rk4_sixth(x1[u] + kv[u]);
               if (i0 + u < NP) {
                 const float dn = gs[i0 + u] - o0[u];
                 red_a = fmaf(dn, dn, red_a);
