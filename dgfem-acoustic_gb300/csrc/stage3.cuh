@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
           const float4 xu = __ldcs(reinterpret_cast<const float4*>(a.u + gidx));
           const float4 xa = __ldcs(reinterpret_cast<const float4*>(a.acc + gidx));
           const float4 xs = __ldcs(reinterpret_cast<const float4*>(a.snap + gidx));
-          const float un[4] = {xu.x + (xa.x + kv.x) / 6.f, xu.y + (xa.y + kv.y) / 6.f, xu.z + (xa.z + kv.z) / 6.f,
-                               xu.w + (xa.w + kv.w) / 6.f};
+          const float un[4] = {xu.x + rk4_sixth(xa.x + kv.x), xu.y + rk4_sixth(xa.y + kv.y),
+                               xu.z + rk4_sixth(xa.z + kv.z), xu.w + rk4_sixth(xa.w + kv.w)};
           const float sn[4] = {xs.x, xs.y, xs.z, xs.w};
 #pragma unroll
           for (int v = 0; v < 4; ++v) racc.add(q, sn[v], un[v], a.c0sq);
