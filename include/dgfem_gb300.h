@@ -155,8 +155,9 @@ int dg_vtu_writer_destroy(dg_vtu_writer* w);
 const char* dg_vtu_writer_last_error(const dg_vtu_writer* w);
 int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* compressed);
 
-/* Stage kernel selection. variant -2: time every variant on this mesh and
- * keep the fastest; -3: the same, unless the tune cache holds a result for
+/* Stage kernel selection. variant -2: time every variant on this mesh (the
+ * four RK stages of a step; the state is left untouched, the stage buffers
+ * and the accumulator are cleared) and keep the fastest; -3: the same, unless the tune cache holds a result for
  * this GPU model, element type, precision and mesh size class (what
  * dg_create does; the environment variable DGFEM_STAGE_VARIANT overrides it
  * there); -1: baseline kernel; k >= 0:
