@@ -20,7 +20,6 @@
 
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "../../include/dgfem_gb300.h"
@@ -34,13 +33,9 @@ namespace {
 constexpr int kChunk = 16384;      // nodes of one variable reduced by one block
 constexpr int kMaxChunks = 4096;   // rows of the scratch array
 constexpr int kThreads = 256;
-constexpr int kMaxDevices = 64;
 
 // Shared by every call on a device; the last call's partial sums stay here.
 static __device__ __align__(256) double g_res_partials[kMaxChunks * 5];
-
-std::mutex g_mu;
-double* g_scratch[kMaxDevices] = {};  // device address of g_res_partials per device
 
 template <typename T>
 __global__ void k_res_partials(const T* u, const T* snap, int n_var, int64_t n, int64_t stride, double c0sq,
@@ -84,21 +79,15 @@ __global__ void k_res_final(const double* part, int nchunks, double inv_n, doubl
   if (lane == 0) out[c] = x * inv_n;
 }
 
-// Device address of the scratch array for the current device (looked up once
-// per device, with that device current).
+// Device address of the scratch array for the current device, looked up on
+// every call with that device current. The lookup allocates nothing, and not
+// caching it keeps the address right after a cudaDeviceReset (which reloads
+// the module, so the array may move).
 cudaError_t scratch_for_current_device(double** p) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* a = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&a, g_res_partials);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch[dev]) {
-    void* a = nullptr;
-    e = cudaGetSymbolAddress(&a, g_res_partials);
-    if (e != cudaSuccess) return e;
-    g_scratch[dev] = static_cast<double*>(a);
-  }
-  *p = g_scratch[dev];
+  *p = static_cast<double*>(a);
   return cudaSuccess;
 }
 

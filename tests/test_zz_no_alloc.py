@@ -62,6 +62,54 @@ def test_noalloc_residuals_match_dg_run_on_two_calls(pkg, dim):
     assert res1[0][0] != res2[0][0]
 
 
+def _residuals_f64(u, snap, n_var, n, c0):
+    """The five residual means (src/solver.cpp:518-545) in float64 numpy."""
+    out = np.zeros(5)
+    c0sq = c0 * c0
+    for q in range(n_var):
+        s, v = snap[q, :n].astype(np.float64), u[q, :n].astype(np.float64)
+        if q == 0:
+            out[0] = np.sum((s - v) ** 2) / n
+            out[1] = np.sum((s / c0sq - v / c0sq) ** 2) / n
+        else:
+            out[1 + q] = np.sum((s - v) ** 2) / n
+    return out
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_noalloc_several_chunks_padded_planes_larger_call_first(pkg, prec):
+    """Inputs spanning several of the kernel's fixed node chunks (a partial
+    last chunk), variable planes longer than the node count, and a smaller
+    call after a larger one: the smaller call must not read the scratch rows
+    the larger call left behind."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    dt = np.float64 if prec == "fp64" else np.float32
+    tdt = torch.float64 if prec == "fp64" else torch.float32
+    flag = pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32
+    c0 = 340.0
+    d_out = torch.full((5,), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    # (nodes per variable, plane stride, variables): 4 chunks then 2 chunks
+    for n, stride, nv in ((50_000, 50_021, 4), (20_000, 20_013, 3)):
+        u = rng.standard_normal((nv, stride)).astype(dt)
+        snap = (u + 0.01 * rng.standard_normal((nv, stride))).astype(dt)
+        # the padding past n holds large values that must not enter the sums
+        u[:, n:] = 1e6
+        snap[:, n:] = -1e6
+        d_u = torch.tensor(u.reshape(-1), dtype=tdt, device="cuda")
+        d_s = torch.tensor(snap.reshape(-1), dtype=tdt, device="cuda")
+        for _ in range(2):
+            pkg.gpu.residuals_noalloc(d_u.data_ptr(), d_s.data_ptr(), flag, nv, n, stride, c0, d_out.data_ptr(),
+                                      stream)
+            torch.cuda.synchronize()
+            got = d_out.cpu().numpy()
+            ref = _residuals_f64(u, snap, nv, n, c0)
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=0.0)
+        if nv == 3:
+            assert got[4] == 0.0
+
+
 def test_noalloc_rejects_inputs_beyond_its_scratch(pkg):
     torch = pytest.importorskip("torch")
     d = torch.zeros(8, dtype=torch.float64, device="cuda")
