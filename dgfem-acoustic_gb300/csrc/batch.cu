@@ -168,6 +168,7 @@ int build_fused_graph(dg_batch* b) {
     dgk::MultiArgs m{};
     m.ntiles_total = 0;
     m.queue = b->d_queue + (st - 1);
+    m.wait_limit = dgk::kWaitRounds;
     for (int k = 0; k < dgk::kMultiOrders; ++k) {
       m.g[k].stage = st;
       m.g[k].ntiles = 0;
@@ -488,7 +489,10 @@ int dg_batch_run(dg_batch* b, int64_t n_steps, double* obs) {
   int herr = 0;
   for (auto& g : b->groups) {
     BCK(b, cudaMemcpy(&herr, g.ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (herr) return fail(b, DG_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (herr) {
+      BCK(b, cudaMemset(g.ctx->d_err, 0, sizeof(int)));  // the batch stays usable
+      return fail(b, DG_ERR_TIMEOUT, "a bounded device wait gave up");
+    }
   }
   return DG_OK;
 }

@@ -261,6 +261,7 @@ dgk::StageArgs<T> stage_args(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k
   a.stride = c->Epad * c->np;
   a.ntiles = c->variant >= 0 ? (int)(c->Epad / c->s2.et) : (int)c->ntiles;
   a.stage = stage;
+  a.wait_limit = c->wait_limit;
   a.dt = dt;
   a.c0sq = c->c0sq;
   a.ph = c->ph;
@@ -432,7 +433,13 @@ int run_steps(dg_ctx* c, int kind, int64_t n_steps, double dt, double* residuals
   CK(c, cudaStreamSynchronize(c->stream));
   c->step += n_steps;
   if (residuals) std::memcpy(residuals, res.data(), res.size() * sizeof(double));
-  if (herr) return fail(c, DG_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy did not complete)");
+  if (herr) {
+    // the kernels that gave up drained their own copies before exiting; the
+    // flag is cleared so that the context stays usable
+    CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return fail(c, DG_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy did not complete)");
+  }
   for (double v : res)
     if (!std::isfinite(v)) return fail(c, DG_ERR_NONFINITE, "non-finite values in the state (residual is NaN/Inf)");
   return DG_OK;
@@ -1261,6 +1268,18 @@ int dg_tune(dg_ctx* c, int variant) {
   c->info.kernel_variant = c->variant;
   c->info.kernel_grid = c->variant >= 0 ? c->grid2 : c->grid;
   return rc;
+}
+
+int dg_set_wait_limit(dg_ctx* c, int rounds) {
+  if (!c || rounds < 0) return DG_ERR_ARG;
+  c->wait_limit = rounds;
+  // the per-step graph holds the kernel arguments: captured again on the
+  // next run
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  return DG_OK;
 }
 
 int dg_bench_steps(dg_ctx* c, int64_t n_steps, double dt, int64_t flush_bytes, double* step_ms, double* kernel_ms) {

@@ -28,6 +28,7 @@ struct dg_ctx {
   int variant = -1, grid2 = 0, max_grid = 0;
   dgk::Stage2Info s2{};
   int* d_err = nullptr;  // device error flags of bounded waits
+  int wait_limit = dgk::kWaitRounds;  // polling rounds of a bounded device wait (dg_set_wait_limit)
   size_t tsize = 8;
   void* u = nullptr;     // state            [nv][Epad*np]
   void* acc = nullptr;   // RK accumulator

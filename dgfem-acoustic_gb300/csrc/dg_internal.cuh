@@ -20,6 +20,10 @@
 
 namespace dgk {
 
+// Polling rounds of a bounded device wait (mbarrier try_wait) before it
+// gives up and the kernel reports DG_ERR_TIMEOUT.
+constexpr int kWaitRounds = 1 << 20;
+
 constexpr int kCodeLfMask = 0x3;       // neighbour local face
 constexpr int kCodePermShift = 2;      // corner permutation index (3 bits)
 constexpr int kCodePermMask = 0x7;
@@ -138,6 +142,7 @@ struct StageArgs {
   int64_t cstride;  // ncurved*NP
   int ntiles;
   int stage;       // 0: k only, 1..4: RK4 stages, 5: Euler (y_out = u + k)
+  int wait_limit;  // polling rounds of a bounded device wait before it gives up
   double dt;
   double c0sq;
   Phys ph;
@@ -219,6 +224,7 @@ struct MultiArgs {
   StageArgs<float> g[kMultiOrders];
   int ntiles_total;
   unsigned* queue;
+  int wait_limit;  // polling rounds of a bounded wait for a work item's copies
 };
 int stage_multi_elems_per_tile(int order);
 int stage_multi_blocks_per_sm();

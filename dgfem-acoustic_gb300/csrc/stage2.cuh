@@ -57,10 +57,11 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Bounded wait for the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for the phase with the given parity: at most `limit` polling
+// rounds (none when limit <= 0); false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kWaitRounds) {
   const uint32_t a = smem_u32(bar);
-  for (int it = 0; it < (1 << 20); ++it) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -543,8 +544,9 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
 
   if (active) curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
   // ---- RK update from registers (vectorised when the node chunk allows) ----
-  if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity)) ok = false;
-  if (!active) return;
+  if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity, a.wait_limit)) ok = false;
+  // after a timeout the operand buffer may still be landing: no RK update
+  if (!active || !ok) return;
   const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
   const T* ea = sE + (size_t)NV * ET * NP;
   const T* es = sE + (size_t)2 * NV * ET * NP;
@@ -662,7 +664,11 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
   for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
   for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
   __syncthreads();
-  if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0);
+  // thread 0: barriers whose armed phase was not yet observed complete (bit
+  // i) and that phase's parity (bit 4+i); drained before the block exits
+  uint32_t pend = 0;
+  auto arm = [&](int i, int parity) { pend = (pend & ~(0x11u << i)) | (1u << i) | ((uint32_t)(parity & 1) << (4 + i)); };
+  if (tid == 0 && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x, 0), arm(0, 0);
 
   ResAcc<T> racc;
   bool ok = true;
@@ -671,20 +677,36 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
   for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     const int64_t e0 = (int64_t)tile * ET;
-    if (ok && !mbar_wait(&bar[b], (it >> 1) & 1)) ok = false;
+    const bool got = mbar_wait(&bar[b], (it >> 1) & 1, a.wait_limit);
+    if (!got) ok = false;
     T* sY = sYb + (size_t)b * NV * ET * NP;
     const T* sGF = sGFb + (size_t)b * ET * RECF;
     const int* sGI = sGIb + (size_t)b * ET * RECI;
     if (tid == 0) {
-      fence_proxy_async();
-      const int nt = tile + gridDim.x;
-      if (nt < a.ntiles) issue_tile(nt, b ^ 1);
-      if (nepi > 0) issue_epi(tile);
+      if (got) pend &= ~(1u << b);
+      // a block that is giving up issues no further copy; the other buffer
+      // and the operand buffer were released at the previous tile's end
+      if (ok) {
+        fence_proxy_async();
+        const int nt = tile + gridDim.x;
+        if (nt < a.ntiles) issue_tile(nt, b ^ 1), arm(b ^ 1, (it + 1) >> 1);
+        if (nepi > 0) issue_epi(tile), arm(2, it);
+      }
     }
     pipe_tile<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
-    __syncthreads();  // buffers of this tile are free again
+    if (tid == 0 && ok) pend &= ~4u;  // thread 0 observed the operand copies (inside the tile)
+    if (__syncthreads_or(!ok)) {      // buffers of this tile are free again
+      ok = false;
+      break;
+    }
   }
-  if (!ok) atomicOr(err, 1);
+  if (tid == 0) {
+    // after a timeout: bounded waits (full limit) for the copies still in
+    // flight, so that none lands in shared memory after the block has left
+    for (int i = 0; i < 3; ++i)
+      if (pend & (1u << i)) mbar_wait(&bar[i], (pend >> (4 + i)) & 1u);
+    if (!ok) atomicOr(err, 1);
+  }
 
   if (stage == 4) {
 #pragma unroll

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(C3Cfg<D, P, NC_, EG_>::NT) stage3_kernel(const
   for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     const int64_t e0 = (int64_t)tile * ET;
-    const bool got = mbar_wait(&bar[b], (it >> 1) & 1);
+    const bool got = mbar_wait(&bar[b], (it >> 1) & 1, a.wait_limit);
     if (tid == 0 && got) pend &= ~(1u << b);
     if (__syncthreads_or(!got)) {
       ok = false;

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(
     const int item = *sItem;  // written before the barrier that ended the previous item
     if (item >= m.ntiles_total) break;
     const int b = it & 1;
-    const bool got = mbar_wait(&bar[b], (it >> 1) & 1);
+    const bool got = mbar_wait(&bar[b], (it >> 1) & 1, m.wait_limit);
     if (tid == 0 && got) pend &= ~(1u << b);
     if (__syncthreads_or(!got)) {
       ok = false;

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
   for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     const int64_t e0 = (int64_t)tile * ET;
-    bool got = mbar_wait(&bar[b], (it >> 1) & 1);
+    bool got = mbar_wait(&bar[b], (it >> 1) & 1, a.wait_limit);
     if (tid == 0 && got) seen(b);
     if (__syncthreads_or(!got)) {
       ok = false;
@@ -462,10 +462,10 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
       umma_commit(&bar[3]);
       arm(3, it);
     }
-    got = mbar_wait(&bar[3], it & 1);
+    got = mbar_wait(&bar[3], it & 1, a.wait_limit);
     if (tid == 0 && got) seen(3);
     if (nepi > 0 && got) {
-      got = mbar_wait(&bar[2], it & 1);
+      got = mbar_wait(&bar[2], it & 1, a.wait_limit);
       if (tid == 0 && got) seen(2);
     }
     if (__syncthreads_or(!got)) {

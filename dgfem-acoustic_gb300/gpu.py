@@ -19,7 +19,7 @@ ERRORS = {1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_MESH", 4: "DG_ERR_NONFIN
 SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_state", "dg_get_state",
            "dg_set_sources", "dg_set_source_values", "dg_set_observers", "dg_snapshot", "dg_run", "dg_run_euler",
            "dg_step_index", "dg_set_step_index", "dg_rhs", "dg_cell_means", "dg_face_info", "dg_stream",
-           "dg_bench_steps", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_host_alloc", "dg_host_free", "dg_kernel_info", "dg_vtu_writer_create", "dg_vtu_write_async",
+           "dg_bench_steps", "dg_set_wait_limit", "dg_tune", "dg_tune_cache_stats", "dg_tune_cache_clear", "dg_host_alloc", "dg_host_free", "dg_kernel_info", "dg_vtu_writer_create", "dg_vtu_write_async",
            "dg_vtu_writer_flush", "dg_vtu_writer_destroy", "dg_vtu_writer_last_error", "dg_vtu_writer_stats", "dg_residuals_noalloc", "dg_batch_create", "dg_batch_destroy",
            "dg_batch_last_error", "dg_batch_info", "dg_batch_set_state", "dg_batch_get_state",
            "dg_batch_set_sources", "dg_batch_set_observers", "dg_batch_run", "dg_batch_bench", "dg_batch_set_fused",
@@ -79,6 +79,7 @@ def lib():
         L.dg_stream.restype = C.c_void_p
         L.dg_bench_steps.argtypes = [C.c_void_p, I64, D, I64, P(D), P(D)]
         L.dg_tune.argtypes = [C.c_void_p, C.c_int]
+        L.dg_set_wait_limit.argtypes = [C.c_void_p, C.c_int]
         L.dg_tune_cache_stats.argtypes = [P(I64), P(I64), P(I64)]
         L.dg_vtu_writer_create.argtypes = [C.c_void_p, I64, P(D), P(I64), C.c_int, C.c_int, P(C.c_void_p)]
         L.dg_vtu_write_async.argtypes = [C.c_void_p, C.c_char_p]
@@ -284,6 +285,11 @@ class Solver:
         the baseline or variant k."""
         self._ck(lib().dg_tune(self.h, variant), "dg_tune")
         return self.info()["kernel_variant"]
+
+    def set_wait_limit(self, rounds):
+        """Polling rounds of each bounded device wait before it gives up
+        (default 2**20); a run whose wait gives up raises DG_ERR_TIMEOUT."""
+        self._ck(lib().dg_set_wait_limit(self.h, rounds), "dg_set_wait_limit")
 
     def stream(self):
         return lib().dg_stream(self.h)

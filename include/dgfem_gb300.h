@@ -170,6 +170,17 @@ int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* com
  * precision. */
 int dg_tune(dg_ctx* ctx, int variant);
 
+/* Polling rounds that each bounded device wait of the stage kernels (the
+ * mbarrier waits for their TMA copies and tensor-core work) makes before it
+ * gives up (default 2^20; 0 gives up at once). A kernel whose wait gives up
+ * issues no further copy, waits with the default limit for the copies it
+ * already issued, sets the context's error flag and returns; the dg_run call
+ * then returns DG_ERR_TIMEOUT and clears the flag, and the context stays
+ * usable. For tests of that failure path and for diagnosing a stalled
+ * device. No reference counterpart (the reference aborts through
+ * Fatal_Error, include/err.h:5-9). */
+int dg_set_wait_limit(dg_ctx* ctx, int rounds);
+
 /* Page-locked (pinned) host memory for the host arrays of dg_set_state,
  * dg_get_state, dg_run and friends: copies from and to it run at the
  * host-device link's rate instead of through a staging buffer. No reference
@@ -220,12 +231,14 @@ int dg_bench_steps(dg_ctx* ctx, int64_t n_steps, double dt, int64_t flush_bytes,
  *
  * Its only scratch is a fixed 160 KiB array inside the library that every GPU
  * loading the library holds until the process exits; n_per_var is therefore
- * limited to 67,108,864 nodes (DG_ERR_ARG beyond). The first call on a device
- * looks up that array's device address with the device current; make that
- * first call before any stream capture. All calls share the array, so calls
- * that overlap on the GPU (concurrent streams) race; calls in one stream are
- * safe back to back (each call writes every scratch row it reads). Errors are
- * reported through dg_last_error(NULL). */
+ * limited to 67,108,864 nodes (DG_ERR_ARG beyond). Every call looks up that
+ * array's device address with the calling thread's current device (so a
+ * cudaDeviceReset between calls is harmless); the first call on a device may
+ * load the library's device code, so make it before any stream capture. All
+ * calls share the array, so calls that overlap on the GPU (concurrent
+ * streams) race; calls in one stream are safe back to back (each call writes
+ * every scratch row it reads). Errors are reported through
+ * dg_last_error(NULL). */
 int dg_residuals_noalloc(const void* u, const void* snap, int precision, int n_var, int64_t n_per_var,
                          int64_t var_stride, double c0, double* res, void* stream);
 
