@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures of the reference's 2d_hilltop case and its
 1-D example mesh.
 
-Reads, from a checkout of the reference (default /root/reference):
+Reads, from a checkout of the reference (the path given as the only
+argument):
   residuals.csv                          per-step residual trace of a reference run
   cases/2d_hilltop/2d_hilltop_fs.msh     its mesh
   cases/2d_hilltop/2d_hilltop.json       its configuration
@@ -20,7 +21,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref="/root/reference"):
+def main(ref):
     rows = open(os.path.join(ref, "residuals.csv")).read().strip().splitlines()
     with open(os.path.join(HERE, "hilltop_residuals.csv"), "w") as f:
         f.write("time;res_p;res_rho;res_vx;res_vy\n")
@@ -40,4 +41,6 @@ def main(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of a checkout of the reference>")
+    main(sys.argv[1])
