@@ -678,20 +678,23 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     const int b = it & 1;
     const int64_t e0 = (int64_t)tile * ET;
     const bool got = mbar_wait(&bar[b], (it >> 1) & 1, a.wait_limit);
-    if (!got) ok = false;
+    if (tid == 0 && got) pend &= ~(1u << b);
+    // a tile whose copy has not arrived holds no valid neighbour indices: the
+    // whole block stops before anything reads them (and issues no copy)
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
     T* sY = sYb + (size_t)b * NV * ET * NP;
     const T* sGF = sGFb + (size_t)b * ET * RECF;
     const int* sGI = sGIb + (size_t)b * ET * RECI;
     if (tid == 0) {
-      if (got) pend &= ~(1u << b);
-      // a block that is giving up issues no further copy; the other buffer
-      // and the operand buffer were released at the previous tile's end
-      if (ok) {
-        fence_proxy_async();
-        const int nt = tile + gridDim.x;
-        if (nt < a.ntiles) issue_tile(nt, b ^ 1), arm(b ^ 1, (it + 1) >> 1);
-        if (nepi > 0) issue_epi(tile), arm(2, it);
-      }
+      // the other buffer and the operand buffer were released at the
+      // previous tile's end
+      fence_proxy_async();
+      const int nt = tile + gridDim.x;
+      if (nt < a.ntiles) issue_tile(nt, b ^ 1), arm(b ^ 1, (it + 1) >> 1);
+      if (nepi > 0) issue_epi(tile), arm(2, it);
     }
     pipe_tile<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     if (tid == 0 && ok) pend &= ~4u;  // thread 0 observed the operand copies (inside the tile)
