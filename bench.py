@@ -225,15 +225,16 @@ def recorded(name):
 
 def tc_mma_flops_per_step(E, dim, order):
     """MMA work of the tensor-core stage kernel per RK4 step: per tile of 32
-    elements three kind::tf32 products (M = 128, N = Np rounded to 16, K = the
-    padded volume and face columns) in each of the four stages."""
+    elements four kind::tf32 products of the split operands (M = 128, N = Np
+    rounded to 16, K = the padded volume and face columns) in each of the
+    four stages."""
     from math import comb
     NP = comb(order + dim, dim)
     NK = (dim + 1) * comb(order + dim - 1, dim - 1)
     NN = (NP + 15) // 16 * 16
     NPP = (NP + 3) // 4 * 4
     KT = (dim * NPP + (NK + 3) // 4 * 4 + 7) // 8 * 8
-    return 4 * ((E + 31) // 32) * 3 * 2 * 128 * NN * KT
+    return 4 * ((E + 31) // 32) * 4 * 2 * 128 * NN * KT
 
 
 def run_plain(args, W, rank, world):
@@ -322,7 +323,7 @@ def run_plain(args, W, rank, world):
     if 16 <= variant < 32:  # tensor-core kernels
         f = tc_mma_flops_per_step(E, 3, W["order"])
         line["tensor_core"] = {"mma_tflops": f / (kern_ms * 1e-3) / 1e12, "mma_flops_per_step": f,
-                               "note": "3 kind::tf32 products per operand pair"}
+                               "note": "4 kind::tf32 products per operand pair (head and tail of each operand)"}
     if args.variants:
         per_variant = {}
         for v in [-1] + list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)):
@@ -536,46 +537,64 @@ def run_precision(args):
     configuration (config 2: 2000 steps, config 3: 500 steps), from the same
     zero initial state driven by the workload's sources: relative L2 of the
     final pressure, the velocity and the whole state, and of the observer
-    traces (pressure and velocity at every step)."""
+    traces (pressure and velocity at every step). FP64 runs once with its
+    autotuned kernel; FP32 runs with its autotuned kernel and with every
+    stage-kernel variant listed in --fp32-variants."""
     pkg = _pkg()
     out = {}
+    extra = [int(v) for v in args.fp32_variants.split(",") if v]
     for key in [k for k in args.configs.split(",") if k]:
         W = WORKLOADS[key]
         nsteps = args.steps if args.steps_override else PRECISION_RUNS[key]
         mesh, dt, srcs, obs = build_problem(W)
         E, np_ = mesh["elem_nodes"].shape
         sdofs, odofs, ows = node_sets(mesh, srcs, obs)
-        runs = {}
-        for prec in ("fp64", "fp32"):
+
+        def run(prec, variant):
             t0 = time.perf_counter()
             S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"],
                                precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32)
+            if variant is not None:
+                if variant >= 0 and S.kernel_info(variant)[0] == 0:
+                    S.close()
+                    return None
+                S.tune(variant)
             S.set_sources(sdofs)
             S.set_source_values(source_values(srcs, nsteps + 2, dt))
             S.set_observers(odofs, ows)
             S.set_state(np.zeros((4, E * np_)))
             S.snapshot()
-            tr = []
-            done = 0
+            tr, done = [], 0
             while done < nsteps:
                 k = min(100, nsteps - done)
                 _, o = S.run(k, dt)
                 tr.append(o)
                 done += k
-            runs[prec] = dict(state=S.get_state(), obs=np.concatenate(tr), s=time.perf_counter() - t0,
-                              variant=S.info()["kernel_variant"])
+            r = dict(state=S.get_state(), obs=np.concatenate(tr), s=time.perf_counter() - t0,
+                     variant=S.info()["kernel_variant"])
             S.close()
-        a, b = runs["fp32"], runs["fp64"]
+            return r
+
+        ref = run("fp64", None)
         rl = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
-        out[key] = {"workload": W["name"], "steps": nsteps, "dt": dt,
-                    "rel_l2_p": rl(a["state"][0], b["state"][0]), "rel_l2_velocity": rl(a["state"][1:], b["state"][1:]),
-                    "rel_l2_state": rl(a["state"], b["state"]),
-                    "rel_l2_observer_p": rl(a["obs"][:, :, 0], b["obs"][:, :, 0]),
-                    "rel_l2_observer_velocity": rl(a["obs"][:, :, 1:], b["obs"][:, :, 1:]),
-                    "max_abs_p_fp64": float(np.abs(b["state"][0]).max()),
-                    "variant_fp32": a["variant"], "variant_fp64": b["variant"],
-                    "wall_s_fp32": round(a["s"], 1), "wall_s_fp64": round(b["s"], 1)}
-        del runs, mesh
+        fp32 = {}
+        for v in [None] + extra:
+            a = run("fp32", v)
+            if a is None:
+                continue
+            fp32[str(a["variant"]) if v is not None else "autotuned(%d)" % a["variant"]] = {
+                "rel_l2_p": rl(a["state"][0], ref["state"][0]),
+                "rel_l2_velocity": rl(a["state"][1:], ref["state"][1:]),
+                "rel_l2_state": rl(a["state"], ref["state"]),
+                "rel_l2_observer_p": rl(a["obs"][:, :, 0], ref["obs"][:, :, 0]),
+                "rel_l2_observer_velocity": rl(a["obs"][:, :, 1:], ref["obs"][:, :, 1:]),
+                "wall_s": round(a["s"], 1)}
+        auto = [k for k in fp32 if k.startswith("autotuned")][0]
+        out[key] = dict({"workload": W["name"], "steps": nsteps, "dt": dt, "variant_fp64": ref["variant"],
+                         "wall_s_fp64": round(ref["s"], 1), "max_abs_p_fp64": float(np.abs(ref["state"][0]).max()),
+                         "fp32_variant": int(auto.split("(")[1].rstrip(")")), "fp32_by_variant": fp32},
+                        **fp32[auto])
+        del ref, mesh
     return {"metric": "FP32 vs FP64 relative L2 after the full run", "runs": out}
 
 
@@ -692,6 +711,7 @@ def main():
     ap.add_argument("--workload", default="scale", choices=["scale", "cube", "ensemble", "surrogate", "precision"])
     ap.add_argument("--configs", default="cube,scale", help="precision workload: the configurations to run")
     ap.add_argument("--steps-override", action="store_true", help="precision workload: run --steps steps")
+    ap.add_argument("--fp32-variants", default="", help="precision workload: FP32 stage-kernel variants to run too")
     ap.add_argument("--orders", default="2,3,4",
                     help="ensemble workload: element orders of the instances to keep (profiling subsets)")
     ap.add_argument("--counts", default="", help="profile: cube counts of a smaller box of the same workload")

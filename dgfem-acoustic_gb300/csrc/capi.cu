@@ -273,7 +273,9 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   const dgk::StageArgs<T> a = stage_args<T>(c, stage, y_in, y_out, k_out, dt);
   if (dgk::is_tc_variant(c->variant)) {
     if constexpr (sizeof(T) == 4)
-      return dgk::launch_stage_tc(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream);
+      return dgk::is_tc2_variant(c->variant)
+                 ? dgk::launch_stage_tc2(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream)
+                 : dgk::launch_stage_tc(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
   }
   if (c->variant >= dgk::kStage3Variant) {
@@ -469,8 +471,9 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
     return c->prec == DG_FP32 ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
                               : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (dgk::is_tc_variant(v))
-    return c->prec == DG_FP32 ? dgk::stage_tc_info(c->dim, c->order, dgk::tc_npart(v))
-                              : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
+    return c->prec != DG_FP32        ? dgk::Stage2Info{0, 0, 0, 0, 0, 0}
+           : dgk::is_tc2_variant(v) ? dgk::stage_tc2_info(c->dim, c->order, dgk::tc_npart(v))
+                                    : dgk::stage_tc_info(c->dim, c->order, dgk::tc_npart(v));
   if (c->prec == DG_FP32)
     return c->dim == 1   ? dgk::stage2_info_f32_1d(c->order, v)
            : c->dim == 2 ? dgk::stage2_info_f32_2d(c->order, v)
@@ -481,7 +484,7 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
 }
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
-// kTcVariant and kTcVariant + 1 the tensor-core kernels, kStage3Variant + k
+// kTcVariant .. kTcVariant + 4 the tensor-core kernels, kStage3Variant + k
 // constant-operator variant k (all three FP32).
 bool set_variant(dg_ctx* c, int v) {
   if (v < 0) {
@@ -972,6 +975,15 @@ int dg_set_state(dg_ctx* c, const double* u) {
     for (int64_t i = 3 * c->E * c->np; i < n; ++i)
       if (u[i] != 0.0) return fail(c, DG_ERR_ARG, "2-D state must have vz = 0");
   CK(c, cudaMemcpyAsync(c->d_ref, u, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  // the padding elements past E take part in every stage (their geometry is
+  // zero, so a finite state stays zero there); they are cleared so that a
+  // non-finite state of an earlier run cannot stay behind in them
+  if (c->Epad > c->E) {
+    const size_t w = c->prec == DG_FP32 ? 4 : 8;
+    for (int q = 0; q < c->nv; ++q)
+      CK(c, cudaMemsetAsync((char*)c->u + ((size_t)q * c->Epad + c->E) * c->np * w, 0,
+                            (size_t)(c->Epad - c->E) * c->np * w, c->stream));
+  }
   int64_t m = (int64_t)c->nv * c->E * c->np;
   if (c->prec == DG_FP32)
     k_ref_to_int<float><<<nblk(m, 256), 256, 0, c->stream>>>(c->d_ref, (float*)c->u, c->d_perm, c->E, c->np, c->nv,

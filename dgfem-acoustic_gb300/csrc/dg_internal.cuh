@@ -196,16 +196,22 @@ cudaError_t launch_stage2_f32_1d(int order, int variant, const StageArgs<float>&
 cudaError_t launch_stage2_f64_1d(int order, int variant, const StageArgs<double>& a, int grid, int* err, cudaStream_t s);
 Stage2Info stage2_info_f32_1d(int order, int variant);
 Stage2Info stage2_info_f64_1d(int order, int variant);
-// Tensor-core stage kernel (stage_tc.cuh, FP32 state only): variant ids
-// kTcVariant, kTcVariant + 1, kTcVariant + 2 (2, 4 or 8 threads per tile row:
-// 256, 512 or 1024 per block) of the context's kernel selection.
+// Tensor-core stage kernels (FP32 state only): variant ids kTcVariant,
+// kTcVariant + 1, kTcVariant + 2 of the context's kernel selection are the
+// one-chunk kernel (stage_tc.cuh; 2, 4 or 8 threads per tile row: 256, 512 or
+// 1024 per block), kTcVariant + 3 and kTcVariant + 4 the two-chunk kernel
+// (stage_tc2.cuh, two blocks per SM; 2 or 4 threads per tile row).
 constexpr int kTcVariant = 16;
-constexpr int kTcVariants = 3;
+constexpr int kTcVariants = 5;
 inline bool is_tc_variant(int v) { return v >= kTcVariant && v < kTcVariant + kTcVariants; }
-inline int tc_npart(int v) { return 2 << (v - kTcVariant); }  // 2, 4, 8 threads per tile row
+inline bool is_tc2_variant(int v) { return v >= kTcVariant + 3 && v < kTcVariant + kTcVariants; }
+inline int tc_npart(int v) { return is_tc2_variant(v) ? 2 << (v - kTcVariant - 3) : 2 << (v - kTcVariant); }
 cudaError_t launch_stage_tc(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
                             cudaStream_t s);
 Stage2Info stage_tc_info(int dim, int order, int npart);
+cudaError_t launch_stage_tc2(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
+                             cudaStream_t s);
+Stage2Info stage_tc2_info(int dim, int order, int npart);
 // Constant-operator stage kernel (stage3.cuh, FP32 state only): variant ids
 // kStage3Variant + k of the context's kernel selection; the operators are
 // uploaded to constant memory once per device and element type.

@@ -1,4 +1,5 @@
-// Tensor-core fused RK4 stage kernel (sm_103a, FP32 state, tcgen05 3xTF32).
+// Tensor-core fused RK4 stage kernel (sm_103a, FP32 state, tcgen05 TF32
+// with two-term splits of both operands).
 //
 // Same arithmetic as the reference's per-stage work (src/Mesh.cpp:734-975,
 // src/solver.cpp:38-57, :488-516), written as one small GEMM per tile of
@@ -17,15 +18,18 @@
 //     buffer, as in the pipelined kernel; neighbour traces are gathered with
 //     cp.async and turned into face fluxes in shared memory;
 //   * each thread owns one row (q,e): it computes the row's A entries, splits
-//     each into a TF32 head and an FP32 tail (x = hi + lo) and writes both to
-//     tensor memory (tcgen05.st), so A never occupies shared memory;
-//   * one thread issues the MMAs D = A_lo B_hi + A_hi B_lo + A_hi B_hi
-//     (tcgen05.mma kind::tf32, A from tensor memory, B = [Dt_1..Dt_D | -LIFT]
-//     split the same way and kept in shared memory in the canonical K-major
-//     no-swizzle layout), completion signalled on an mbarrier;
+//     each into a TF32 head and a TF32 tail (x ~ hi + lo, |x - hi - lo| <=
+//     2^-22 |x|) and writes both to tensor memory (tcgen05.st), so A never
+//     occupies shared memory;
+//   * one thread issues the MMAs D = A_lo B_lo + A_lo B_hi + A_hi B_lo +
+//     A_hi B_hi (tcgen05.mma kind::tf32, A from tensor memory, B = [Dt_1..Dt_D
+//     | -LIFT] rounded to 22 significand bits and split exactly into head and
+//     tail, kept in shared memory in the canonical K-major no-swizzle layout),
+//     completion signalled on an mbarrier;
 //   * the epilogue reads the row's accumulator (tcgen05.ld), applies the RK
 //     update in shared memory and writes the tile back with TMA bulk stores.
-// The split keeps about 21 mantissa bits per product (FP32-level results).
+// The products are exact; the errors are the data split (2^-22), the
+// operator's 22-bit rounding (2^-23, fixed) and the FP32 accumulation.
 // Every wait is bounded; on timeout the block records an error flag, waits
 // (bounded) for its own tensor-core work and copies, frees its tensor memory
 // and returns.
@@ -101,13 +105,27 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
-// Splits four values into TF32 heads and FP32 tails.
+// Splits four values into TF32 heads and TF32 tails, both rounded to
+// nearest: x - hi is exact in FP32, and rounding it (instead of letting the
+// MMA drop its low 13 bits) keeps the tail's error unbiased.
 __device__ __forceinline__ void split4(const float* x, uint32_t* hi, uint32_t* lo) {
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
     hi[u] = tf32_rna(x[u]);
-    lo[u] = __float_as_uint(x[u] - __uint_as_float(hi[u]));
+    lo[u] = tf32_rna(x[u] - __uint_as_float(hi[u]));
   }
+}
+
+// An operator entry as an exact pair of TF32 values: x is first rounded to
+// nearest at 22 significand bits (an error of at most 2^-23 |x|, fixed for
+// the whole run), so that head = TF32(x22) and tail = x22 - head (at most 11
+// significand bits) represent it without further error.
+__device__ __forceinline__ void split_op22(float x, uint32_t& hi, uint32_t& lo) {
+  uint32_t u = __float_as_uint(x);
+  u = (u + 1u + ((u >> 2) & 1u)) & ~3u;  // round to nearest even at bit 2
+  const float x22 = __uint_as_float(u);
+  hi = tf32_rna(x22);
+  lo = __float_as_uint(x22 - __uint_as_float(hi));
 }
 
 template <int N, int A>
@@ -286,9 +304,10 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
       }
     }
     const uint32_t off = (uint32_t)((k / 4) * C::NG + n / 8) * 128 + (n % 8) * 16 + (k % 4) * 4;
-    const uint32_t h = tf32_rna(x);
+    uint32_t h, l;
+    split_op22(x, h, l);
     *reinterpret_cast<uint32_t*>(sBh + off) = h;
-    *reinterpret_cast<float*>(sBl + off) = x - __uint_as_float(h);
+    *reinterpret_cast<uint32_t*>(sBl + off) = l;
   }
   for (int i = tid; i < (int)(C::BSLACK / 4); i += NT)
     reinterpret_cast<float*>(sBl + C::BBYTES)[i] = 0.f;
@@ -447,13 +466,13 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
     __syncthreads();
     tc_fence_after();
 
-    // ---- D = A_lo B_hi + A_hi B_lo + A_hi B_hi ----
+    // ---- D = A_lo B_lo + A_lo B_hi + A_hi B_lo + A_hi B_hi (small terms first) ----
     if (tid == 0) {
       const uint32_t bh = smem_u32(sBh), bl = smem_u32(sBl);
 #pragma unroll 1
-      for (int pass = 0; pass < 3; ++pass) {
-        const uint32_t acol = pass == 0 ? C::COL_AL : C::COL_AH;
-        const uint32_t bsrc = pass == 1 ? bl : bh;
+      for (int pass = 0; pass < 4; ++pass) {
+        const uint32_t acol = pass < 2 ? C::COL_AL : C::COL_AH;
+        const uint32_t bsrc = (pass & 1) ? bh : bl;
 #pragma unroll 1
         for (int ks = 0; ks < KT / 8; ++ks)
           umma_tf32_ts(tbase + C::COL_D, tbase + acol + ks * 8, umma_desc(bsrc + ks * 2 * C::LBO, C::LBO, C::SBO),

@@ -163,8 +163,10 @@ int dg_vtu_writer_stats(const dg_vtu_writer* w, int64_t* files_written, int* com
  * there); -1: baseline kernel; k >= 0:
  * pipelined variant k (TMA-staged tiles; the variants differ in output nodes
  * per thread and elements per tile); 16, 17, 18: tensor-core kernel with 256,
- * 512 or 1024 threads per block (FP32 contexts only: tcgen05 MMAs with a
- * 3xTF32 split, FP32-level results); 32 + k: constant-operator variant k (FP32
+ * 512 or 1024 threads per block (FP32 contexts only: tcgen05 TF32 MMAs of
+ * head/tail-split operands, FP32-level results); 19, 20: the two-chunk
+ * tensor-core kernel (K applied in at most two chunks so that two blocks
+ * share an SM) with 256 or 512 threads per block (FP32 only); 32 + k: constant-operator variant k (FP32
  * contexts only: operators in constant memory). Returns
  * DG_ERR_ARG for a variant that does not exist for this element type or
  * precision. */

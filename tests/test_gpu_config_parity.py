@@ -111,7 +111,7 @@ def test_config1_fp64_full_run_matches_oracle(pkg, config1, variant):
     assert e["residuals"] <= 1e-10, (out["variant"], e)
 
 
-@pytest.mark.parametrize("variant", [None, 0, 1, 2, 32, 33, 34, 16])
+@pytest.mark.parametrize("variant", [None, 0, 1, 2, 32, 33, 34, 16, 19])
 def test_config1_fp32_full_run_within_1e5_of_fp64_oracle(pkg, config1, variant):
     out = _run(pkg, config1, pkg.gpu.DG_FP32, variant)
     if out is None:

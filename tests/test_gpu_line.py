@@ -56,7 +56,7 @@ def test_line_rhs_matches_oracle(pkg, oracle, p, prec):
     ref = oracle.Problem(mesh, dt=dt, **PHYS1).stage(u)
     S = pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **PHYS1)
     tol = 5e-11 if prec == "fp64" else 5e-4
-    variants = [v for v in [-1, 0, 1, 16, 17, 18, 32] if v < 0 or S.kernel_info(v)[0] > 0]
+    variants = [v for v in [-1, 0, 1, 16, 17, 18, 19, 20, 32] if v < 0 or S.kernel_info(v)[0] > 0]
     assert variants == [-1, 0]
     for v in variants:
         S.tune(v)

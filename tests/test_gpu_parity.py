@@ -32,7 +32,7 @@ def kernel_variants(pkg, S):
     """-1 (baseline kernel) and every other stage-kernel variant available
     for S: pipelined (0..), tensor-core (16-18), constant-operator (32..)."""
     out = [-1]
-    for v in list(range(8)) + [16, 17, 18] + list(range(32, 40)):
+    for v in list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)):
         if S.kernel_info(v)[0] > 0:
             out.append(v)
     return out

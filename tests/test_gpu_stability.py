@@ -33,14 +33,14 @@ def test_cube_workload_stays_bounded(pkg):
     spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
     bench = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bench)
-    mesh, dt, src, obs = bench.build_problem()
-    W = bench.WORKLOAD
+    W = bench.CUBE
+    mesh, dt, srcs, obs = bench.build_problem(W)
+    src = srcs[0]
     S = pkg.gpu.Solver(mesh, v0=W["v0"], rho0=W["rho0"], c0=W["c0"], precision=pkg.gpu.DG_FP32)
-    sd, od, ow = bench.node_sets(mesh, src, obs)
+    sd, od, ow = bench.node_sets(mesh, srcs, obs)
     S.set_sources(sd)
     n = 2000
-    t = np.arange(n + 1) * dt
-    S.set_source_values((src[4] * np.sin(2 * np.pi * src[5] * t + src[6]))[:, None])
+    S.set_source_values(bench.source_values(srcs, n + 1, dt))
     S.set_observers(od, ow)
     S.snapshot()
     peak = 0.0

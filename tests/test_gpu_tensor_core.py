@@ -1,11 +1,14 @@
-"""The tensor-core stage kernel (tcgen05, 3xTF32 split, FP32 state) and the
-Euler1 integrator against the CPU oracle, through the C ABI.
+"""The tensor-core stage kernels (tcgen05 TF32 MMAs of head/tail-split
+operands, FP32 state) and the Euler1 integrator against the CPU oracle,
+through the C ABI.
 
-The tensor-core kernel is kernel variant 16, 17 or 18 (256, 512 or 1024
-threads per block: each tile row's columns split 2, 4 or 8 ways) of an FP32
-context. Its products
-keep about 21 mantissa bits (x = tf32 head + fp32 tail, the tail-tail product
-dropped), so it is held to the same bounds as the CUDA-core FP32 kernels: a
+The tensor-core kernels are kernel variants 16, 17 or 18 (one-chunk kernel,
+256, 512 or 1024 threads per block: each tile row's columns split 2, 4 or 8
+ways) and 19 or 20 (two-chunk kernel, two blocks per SM: K applied in at most
+two chunks, 256 or 512 threads per block) of an FP32 context. Each operand is
+a TF32 head plus a TF32 tail (the operator rounded to 22 significand bits so
+that the pair is exact; the data within 2^-22), four products summed in
+FP32, so they are held to the same bounds as the CUDA-core FP32 kernels: a
 single right-hand side within the FP32 single-RHS bound of the oracle and
 within a few times the CUDA-core kernel's own error; a full run within 1e-5
 relative L2 of the FP64 oracle on the state and the observer traces."""
@@ -20,6 +23,8 @@ pytestmark = pytest.mark.gpu
 TC = 16
 TC4 = 17
 TC8 = 18
+TC2 = 19
+TC2_4 = 20
 
 
 def _obs_err(tr, ref_obs):
@@ -34,7 +39,7 @@ def _solver(pkg, mesh, ph, prec="fp32"):
     return pkg.gpu.Solver(mesh, precision=pkg.gpu.DG_FP64 if prec == "fp64" else pkg.gpu.DG_FP32, **ph)
 
 
-@pytest.mark.parametrize("tc", [TC, TC4, TC8])
+@pytest.mark.parametrize("tc", [TC, TC4, TC8, TC2, TC2_4])
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
 def test_tc_rhs_matches_oracle(pkg, oracle, dim, p, tc):
@@ -59,7 +64,7 @@ def test_tc_rhs_matches_oracle(pkg, oracle, dim, p, tc):
 def test_tc_not_offered_in_fp64(pkg):
     mesh = _mesh(pkg, 2, 2)
     S = _solver(pkg, mesh, _phys(2), "fp64")
-    for tc in (TC, TC4, TC8):
+    for tc in (TC, TC4, TC8, TC2, TC2_4):
         with pytest.raises(pkg.gpu.SolverError):
             S.tune(tc)
 
@@ -98,7 +103,8 @@ def _run(pkg, oracle, mesh, ph, prec, variant, nsteps, euler=False):
 
 
 @pytest.mark.parametrize("dim,p,tc", [(2, 2, TC), (2, 3, TC), (2, 4, TC), (3, 2, TC), (3, 3, TC), (3, 4, TC),
-                                      (2, 3, TC4), (3, 3, TC4), (3, 4, TC8)])
+                                      (2, 3, TC4), (3, 3, TC4), (3, 4, TC8), (2, 2, TC2), (2, 4, TC2),
+                                      (3, 2, TC2), (3, 3, TC2), (3, 4, TC2), (3, 4, TC2_4), (2, 3, TC2_4)])
 def test_tc_run_matches_oracle(pkg, oracle, dim, p, tc):
     mesh = _mesh(pkg, dim, p)
     u, res, tr, ref = _run(pkg, oracle, mesh, _phys(dim), "fp32", tc, 40)
@@ -108,7 +114,7 @@ def test_tc_run_matches_oracle(pkg, oracle, dim, p, tc):
     assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= 1e-4
 
 
-@pytest.mark.parametrize("prec,variant", [("fp64", -1), ("fp64", 0), ("fp32", 1), ("fp32", TC)])
+@pytest.mark.parametrize("prec,variant", [("fp64", -1), ("fp64", 0), ("fp32", 1), ("fp32", TC), ("fp32", TC2)])
 @pytest.mark.parametrize("dim,p", [(2, 3), (3, 3)])
 def test_euler_run_matches_oracle(pkg, oracle, dim, p, prec, variant):
     mesh = _mesh(pkg, dim, p)
@@ -120,16 +126,19 @@ def test_euler_run_matches_oracle(pkg, oracle, dim, p, prec, variant):
     assert _obs_err(tr, ref["obs"][:, :, [1, 2, 3, 4]]) <= tol * 10
 
 
-@pytest.mark.parametrize("tc", [TC, TC4, TC8])
-def test_tc_many_tiles_per_block(pkg, oracle, tc):
+@pytest.mark.parametrize("tc,p", [(TC, 3), (TC4, 3), (TC8, 3), (TC2, 3), (TC2_4, 3), (TC, 4), (TC2, 4), (TC2_4, 4)])
+def test_tc_many_tiles_per_block(pkg, oracle, tc, p):
     """A mesh with more tiles than resident blocks, so that every block walks
-    several tiles through both halves of its double buffer: one RHS against
-    the oracle and 20 RK4 steps against the CUDA-core FP32 kernel."""
+    several tiles through its tile buffers (at p = 4 the two-chunk kernel
+    applies K in two chunks): one RHS against the oracle, and 20 RK4 steps of
+    the tensor-core and the CUDA-core FP32 kernels against an FP64 run of the
+    same steps (the tensor-core run within the FP32 bound and within a few
+    times the CUDA-core kernel's own error)."""
     mg = pkg.meshgen
-    m = mg.box(counts=(14, 14, 14), order=3, seed=21)
+    m = mg.box(counts=(14, 14, 14) if p == 3 else (12, 12, 12), order=p, seed=21)
     bcs = {"xmin": "Reflecting", "xmax": "Reflecting", "ymin": "Absorbing", "ymax": "Absorbing",
            "zmin": "Absorbing", "zmax": "Absorbing"}
-    mesh = dict(dim=3, order=3, xyz=m["xyz"], elem_nodes=m["elem_nodes"], groups=mg.solver_groups(m, bcs))
+    mesh = dict(dim=3, order=p, xyz=m["xyz"], elem_nodes=m["elem_nodes"], groups=mg.solver_groups(m, bcs))
     ph = _phys(3)
     u0 = smooth_state(mesh, seed=77)
     dt = 2e-5
@@ -144,5 +153,12 @@ def test_tc_many_tiles_per_block(pkg, oracle, tc):
         S.snapshot()
         r, _ = S.run(20, dt)
         out.append((S.get_state(), r))
-    assert rel_l2(out[1][0][:4], out[0][0][:4]) <= 1e-6
-    np.testing.assert_allclose(out[1][1][:, :4], out[0][1][:, :4], rtol=1e-3, atol=0)
+    S64 = _solver(pkg, mesh, ph, "fp64")
+    S64.set_state(u0)
+    S64.snapshot()
+    r64, _ = S64.run(20, dt)
+    u64 = S64.get_state()
+    S64.close()
+    err_cc, err_tc = rel_l2(out[0][0][:4], u64[:4]), rel_l2(out[1][0][:4], u64[:4])
+    assert err_tc <= 1e-5 and err_tc <= 4 * err_cc + 1e-6, (err_tc, err_cc)
+    np.testing.assert_allclose(out[1][1][:, :4], r64[:, :4], rtol=1e-3, atol=0)
