@@ -225,7 +225,7 @@ def recorded(name):
 
 def tc_mma_flops_per_step(E, dim, order):
     """MMA work of the tensor-core stage kernel per RK4 step: per tile of 32
-    elements four kind::tf32 products of the split operands (M = 128, N = Np
+    elements three kind::tf32 products of the split operands (M = 128, N = Np
     rounded to 16, K = the padded volume and face columns) in each of the
     four stages."""
     from math import comb
@@ -234,7 +234,7 @@ def tc_mma_flops_per_step(E, dim, order):
     NN = (NP + 15) // 16 * 16
     NPP = (NP + 3) // 4 * 4
     KT = (dim * NPP + (NK + 3) // 4 * 4 + 7) // 8 * 8
-    return 4 * ((E + 31) // 32) * 4 * 2 * 128 * NN * KT
+    return 4 * ((E + 31) // 32) * 3 * 2 * 128 * NN * KT
 
 
 def run_plain(args, W, rank, world):
@@ -323,7 +323,7 @@ def run_plain(args, W, rank, world):
     if 16 <= variant < 32:  # tensor-core kernels
         f = tc_mma_flops_per_step(E, 3, W["order"])
         line["tensor_core"] = {"mma_tflops": f / (kern_ms * 1e-3) / 1e12, "mma_flops_per_step": f,
-                               "note": "4 kind::tf32 products per operand pair (head and tail of each operand)"}
+                               "note": "3 kind::tf32 products per operand pair (head x head and the two head x tail corrections)"}
     if args.variants:
         per_variant = {}
         for v in [-1] + list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)):

@@ -21,15 +21,16 @@
 //     each into a TF32 head and a TF32 tail (x ~ hi + lo, |x - hi - lo| <=
 //     2^-22 |x|) and writes both to tensor memory (tcgen05.st), so A never
 //     occupies shared memory;
-//   * one thread issues the MMAs D = A_lo B_lo + A_lo B_hi + A_hi B_lo +
-//     A_hi B_hi (tcgen05.mma kind::tf32, A from tensor memory, B = [Dt_1..Dt_D
-//     | -LIFT] rounded to 22 significand bits and split exactly into head and
-//     tail, kept in shared memory in the canonical K-major no-swizzle layout),
-//     completion signalled on an mbarrier;
+//   * one thread issues the MMAs D = A_lo B_hi + A_hi B_lo + A_hi B_hi, the
+//     correction products first while D is small (tcgen05.mma kind::tf32, A
+//     from tensor memory, B = [Dt_1..Dt_D | -LIFT] rounded to 22 significand
+//     bits and split exactly into head and tail, kept in shared memory in the
+//     canonical K-major no-swizzle layout), completion signalled on an
+//     mbarrier;
 //   * the epilogue reads the row's accumulator (tcgen05.ld), applies the RK
 //     update in shared memory and writes the tile back with TMA bulk stores.
-// The products are exact; the errors are the data split (2^-22), the
-// operator's 22-bit rounding (2^-23, fixed) and the FP32 accumulation.
+// The errors are the data split (2^-22), the dropped A_lo B_lo (< 2^-22),
+// the operator's 22-bit rounding (2^-23, fixed) and the FP32 accumulation.
 // Every wait is bounded; on timeout the block records an error flag, waits
 // (bounded) for its own tensor-core work and copies, frees its tensor memory
 // and returns.
@@ -466,13 +467,14 @@ __global__ void __launch_bounds__(TcCfg<D, P, NPART>::NT) stage_tc_kernel(const 
     __syncthreads();
     tc_fence_after();
 
-    // ---- D = A_lo B_lo + A_lo B_hi + A_hi B_lo + A_hi B_hi (small terms first) ----
+    // ---- D = A_lo B_hi + A_hi B_lo + A_hi B_hi: the correction products
+    // first, while D is small (each MMA's accumulation rounds relative to D) ----
     if (tid == 0) {
       const uint32_t bh = smem_u32(sBh), bl = smem_u32(sBl);
 #pragma unroll 1
-      for (int pass = 0; pass < 4; ++pass) {
-        const uint32_t acol = pass < 2 ? C::COL_AL : C::COL_AH;
-        const uint32_t bsrc = (pass & 1) ? bh : bl;
+      for (int pass = 0; pass < 3; ++pass) {
+        const uint32_t acol = pass == 0 ? C::COL_AL : C::COL_AH;
+        const uint32_t bsrc = pass == 1 ? bl : bh;
 #pragma unroll 1
         for (int ks = 0; ks < KT / 8; ++ks)
           umma_tf32_ts(tbase + C::COL_D, tbase + acol + ks * 8, umma_desc(bsrc + ks * 2 * C::LBO, C::LBO, C::SBO),

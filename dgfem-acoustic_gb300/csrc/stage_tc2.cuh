@@ -5,16 +5,18 @@
 // Same arithmetic as stage_tc.cuh (the RHS of a tile of ET elements is one
 // GEMM D = A B^T with rows m = (q,e), K = the contravariant volume fluxes
 // (r,j) then the scaled face fluxes k, N = output node i; B = [Dt_1..Dt_D |
-// -LIFT], four TF32 products of the split operands, FP32 accumulate),
+// -LIFT], TF32 products of the split operands, FP32 accumulate),
 // following src/Mesh.cpp:734-975, src/solver.cpp:38-57 and :488-516. What
 // differs is the resource plan. One pipeline per block holds every phase of
 // a tile in sequence (TMA load, neighbour gathers, A construction, MMA,
 // epilogue); at 3-D p = 4 the single block per SM that the one-chunk kernel
 // fits (384 tensor-memory columns, 170 KB of shared memory) left the SM idle
 // through each phase's latency. Here:
-//   * K is applied in chunks of at most KC columns, A (head and tail) for one
-//     chunk at a time, so that a block's tensor memory (D + 2 KC columns) is
-//     at most 256 columns: two blocks per SM, each hiding the other's waits;
+//   * K is applied in at most two chunks, A (head and tail) for one chunk at
+//     a time, so that a block's tensor memory (D + 2 KC columns) is at most
+//     256 columns: two blocks per SM, each hiding the other's waits; the
+//     second chunk's correction products go to a second accumulator in the
+//     A region's free columns (tc2_mma_chunk);
 //   * the tile buffer is single: the next tile's TMA load is issued as soon as
 //     the current tile's stage input has been turned into A and face fluxes
 //     (it overlaps the last MMA chunk and the epilogue);
@@ -56,11 +58,16 @@ struct Tc2Cfg {
   static constexpr int KF = RoundUpTc<NK, 4>::v;         // face columns
   static constexpr int KT = RoundUpTc<KV + KF, 8>::v;    // K (multiple of the TF32 MMA depth 8)
   static constexpr int NN = RoundUpTc<NP, 16>::v;        // N (multiple of 16 for M = 128)
-  // K columns per chunk: D + A head + A tail within 256 columns
+  // K chunks: D + A head + A tail within 256 columns. The first chunk is as
+  // wide as that allows (KC); a second chunk takes the rest (KC2), and its
+  // A leaves room in the A region for a second accumulator DC that takes
+  // its correction products (see tc2_mma_chunk)
   static constexpr int KCMAX = (256 - NN) / 2 / 8 * 8;
-  static constexpr int NCH = (KT + KCMAX - 1) / KCMAX;
-  static constexpr int KC = RoundUpTc<(KT + NCH - 1) / NCH, 8>::v;
+  static constexpr int NCH = KT <= KCMAX ? 1 : 2;
+  static constexpr int KC = NCH == 1 ? KT : KCMAX;
+  static constexpr int KC2 = KT - KC;
   static constexpr int COL_D = 0, COL_AH = NN, COL_AL = NN + KC;  // tensor-memory columns
+  static constexpr int COL_AL2 = NN + KC2, COL_DC = NN + 2 * KC2;  // second chunk: A tail, DC
   static constexpr int TCOLS = Pow2Cols<NN + 2 * KC>::v;
   static constexpr int GT = D * D + D + 1;               // per-element values of the row phase
   static constexpr int VWY = (NP % 4 == 0) ? 4 : (NP % 2 == 0) ? 2 : 1;
@@ -86,7 +93,8 @@ struct Tc2Cfg {
   static constexpr size_t oN = RoundUpTc<oGI + GIB, 128>::v;                   // [NV][ET][NKP]
   static constexpr size_t oR = RoundUpTc<oN + (size_t)NV * ET * NKP * 4, 16>::v;  // [NT/32][5] double
   static constexpr size_t bytes = oR + (NT / 32) * 5 * sizeof(double);
-  static_assert(NCH <= 2 && NCH * KC >= KT, "K must fit in two chunks");
+  static_assert(KT <= 2 * KCMAX, "K must fit in two chunks");
+  static_assert(NCH == 1 || COL_DC + NN <= NN + 2 * KC, "the second accumulator must fit in the A region");
   static_assert(ROWS <= 128, "rows of a tile exceed the MMA height");
   static_assert(NN + 2 * KC <= 256, "tensor memory of a block exceeds 256 columns");
   static_assert(NV * ET * NP <= NV * ET * NKP, "dt*L of a tile must fit in the face buffer");
@@ -101,14 +109,14 @@ struct Tc2Cfg {
 //   Q = 0 (pressure):  gv0_r p_j + sum_d (rho0 c0^2 G_rd) v_d,j
 //   Q = 1+d (v_d):     gv0_r v_d,j + (G_rd / rho0) p_j
 // with gv0_r = sum_d G_rd v0_d, each value split into a TF32 head and a
-// TF32 tail at columns COL_AH / COL_AL + (col - kc0). cf holds the element's
+// TF32 tail at columns COL_AH / col_al + (col - kc0). cf holds the element's
 // coefficients: gv0 (D values), then rho0 c0^2 G (D*D, Q = 0) or G_rQ / rho0
 // (D, Q > 0). The thread takes the 4-node groups j0 = 4*(part + t*NPART);
 // the last group of an NP that is not a multiple of 4 is clamped and padded
 // with zeros.
 template <class C, int Q>
 __device__ __forceinline__ void tc2_build_vol(const float* sY, const float* cf, int e, int part, uint32_t trow,
-                                              int kc0, int kc1) {
+                                              int kc0, int kc1, int col_al) {
   constexpr int D = C::D, NP = C::NP, NPP = C::NPP, ET = C::ET;
   const float* yp_row = sY + e * NP;                               // pressure
   const float* yq_row = sY + (Q == 0 ? 1 : Q) * ET * NP + e * NP;  // v_x (Q = 0) or v_Q
@@ -156,7 +164,7 @@ __device__ __forceinline__ void tc2_build_vol(const float* sY, const float* cf, 
       uint32_t hi[4], lo[4];
       split4(fr, hi, lo);
       tmem_st4(trow + C::COL_AH + (col - kc0), hi);
-      tmem_st4(trow + C::COL_AL + (col - kc0), lo);
+      tmem_st4(trow + col_al + (col - kc0), lo);
     }
   }
 }
@@ -201,13 +209,13 @@ __device__ __forceinline__ void tc2_coeffs(const float* sGT, int q, int e, float
 // tc2_build_vol for the row's variable q (warp-uniform).
 template <class C>
 __device__ __forceinline__ void tc2_build_vol_q(int q, const float* sY, const float* cf, int e, int part,
-                                                uint32_t trow, int kc0, int kc1) {
+                                                uint32_t trow, int kc0, int kc1, int col_al) {
   switch (q) {
-    case 0: tc2_build_vol<C, 0>(sY, cf, e, part, trow, kc0, kc1); break;
-    case 1: tc2_build_vol<C, 1>(sY, cf, e, part, trow, kc0, kc1); break;
-    case 2: tc2_build_vol<C, 2>(sY, cf, e, part, trow, kc0, kc1); break;
+    case 0: tc2_build_vol<C, 0>(sY, cf, e, part, trow, kc0, kc1, col_al); break;
+    case 1: tc2_build_vol<C, 1>(sY, cf, e, part, trow, kc0, kc1, col_al); break;
+    case 2: tc2_build_vol<C, 2>(sY, cf, e, part, trow, kc0, kc1, col_al); break;
     default:
-      if constexpr (C::D == 3) tc2_build_vol<C, 3>(sY, cf, e, part, trow, kc0, kc1);
+      if constexpr (C::D == 3) tc2_build_vol<C, 3>(sY, cf, e, part, trow, kc0, kc1, col_al);
       break;
   }
 }
@@ -216,7 +224,7 @@ __device__ __forceinline__ void tc2_build_vol_q(int q, const float* sY, const fl
 // thread's row from the face-flux plane of variable q.
 template <class C>
 __device__ __forceinline__ void tc2_build_face(const float* sN, int q, int e, int part, uint32_t trow, int kc0,
-                                               int kc1) {
+                                               int kc1, int col_al) {
   constexpr int KV = C::KV, NK = C::NK;
   const float* hrow = sN + (size_t)(q * C::ET + e) * C::NKP;
   for (int c4 = part; c4 < (C::KT - KV) / 4; c4 += C::NPART) {
@@ -228,27 +236,33 @@ __device__ __forceinline__ void tc2_build_face(const float* sN, int q, int e, in
     uint32_t hi[4], lo[4];
     split4(x, hi, lo);
     tmem_st4(trow + C::COL_AH + (col - kc0), hi);
-    tmem_st4(trow + C::COL_AL + (col - kc0), lo);
+    tmem_st4(trow + col_al + (col - kc0), lo);
   }
 }
 
-// One chunk's MMAs (issued by one thread): D (+)= A_lo B_lo + A_lo B_hi +
-// A_hi B_lo + A_hi B_hi over K columns [kc0, kc1) (small terms first), then a
-// commit to bar. With the operator split exactly (split_op22) the four
-// products are exact; what remains is the data split (|x - hi - lo| <=
-// 2^-22 |x|, rounded to nearest) and the FP32 accumulation.
+// One chunk's MMAs (issued by one thread) over K columns [kc0, kc1), then a
+// commit to bar: the correction products A_lo B_hi and A_hi B_lo into the
+// accumulator at column dcorr, then the head products A_hi B_hi into D. Each
+// MMA's FP32 accumulation rounds relative to the accumulator it adds to, so
+// the small correction products must not be added to an accumulator that
+// already holds a large sum: the first chunk adds them to D before its head
+// products (D still small), the second chunk to its own accumulator DC,
+// which the epilogue adds to D. (The operator is split exactly, split_op22;
+// the dropped A_lo B_lo is below 2^-22 of a product.)
 template <class C>
 __device__ __forceinline__ void tc2_mma_chunk(uint32_t tbase, uint32_t bh, uint32_t bl, uint32_t idesc, int kc0,
-                                              int kc1, bool first, uint64_t* bar) {
+                                              int kc1, int col_al, int dcorr, bool first, uint64_t* bar) {
 #pragma unroll 1
-  for (int pass = 0; pass < 4; ++pass) {
-    const uint32_t acol = pass < 2 ? C::COL_AL : C::COL_AH;
-    const uint32_t bsrc = (pass & 1) ? bh : bl;
+  for (int pass = 0; pass < 3; ++pass) {
+    const uint32_t acol = pass == 0 ? col_al : C::COL_AH;
+    const uint32_t bsrc = pass == 1 ? bl : bh;
+    const uint32_t dcol = pass < 2 ? dcorr : C::COL_D;
+    // the first MMA into an accumulator that starts empty overwrites it
+    const bool init0 = (pass == 0 && (first || dcorr != C::COL_D));
 #pragma unroll 1
     for (int ks = 0; ks < (kc1 - kc0) / 8; ++ks)
-      umma_tf32_ts(tbase + C::COL_D, tbase + acol + ks * 8,
-                   umma_desc(bsrc + (kc0 / 8 + ks) * 2 * C::LBO, C::LBO, C::SBO), idesc,
-                   (first && pass == 0 && ks == 0) ? 0u : 1u);
+      umma_tf32_ts(tbase + dcol, tbase + acol + ks * 8, umma_desc(bsrc + (kc0 / 8 + ks) * 2 * C::LBO, C::LBO, C::SBO),
+                   idesc, (init0 && ks == 0) ? 0u : 1u);
   }
   umma_commit(bar);
 }
@@ -480,7 +494,7 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
     if (row_ok) {
       tc2_coeffs<C>(sGT, q, e, rhoc2, inv_rho0, cf);
       // ---- volume columns of the first chunk ----
-      tc2_build_vol_q<C>(q, sY, cf, e, part, trow, 0, KC);
+      tc2_build_vol_q<C>(q, sY, cf, e, part, trow, 0, KC, C::COL_AL);
     }
     // one barrier for both: the first chunk's A is in tensor memory, and
     // every thread's neighbour gathers have landed
@@ -490,7 +504,7 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
     __syncthreads();
     tc_fence_after();
     if constexpr (NCH == 2) {
-      if (leader) tc2_mma_chunk<C>(tbase, bh, bl, idesc, 0, KC, true, &bar[1]), arm(1, mma_phase);
+      if (leader) tc2_mma_chunk<C>(tbase, bh, bl, idesc, 0, KC, C::COL_AL, C::COL_D, true, &bar[1]), arm(1, mma_phase);
     }
     // ---- face numerical fluxes (in place of the gathered traces; they
     // overlap the first chunk's MMAs) ----
@@ -508,18 +522,21 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
         break;
       }
       tc_fence_after();
-      if (row_ok) tc2_build_vol_q<C>(q, sY, cf, e, part, trow, KC, KT);
+      if (row_ok) tc2_build_vol_q<C>(q, sY, cf, e, part, trow, KC, KT, C::COL_AL2);
     } else {
       __syncthreads();  // the face fluxes are in sN
     }
-    if (row_ok) tc2_build_face<C>(sN, q, e, part, trow, NCH == 2 ? KC : 0, KT);
+    if (row_ok) tc2_build_face<C>(sN, q, e, part, trow, NCH == 2 ? KC : 0, KT, NCH == 2 ? C::COL_AL2 : C::COL_AL);
     tmem_wait_st();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     bool gm2 = true;
     if (leader) {
-      tc2_mma_chunk<C>(tbase, bh, bl, idesc, NCH == 2 ? KC : 0, KT, NCH == 1, &bar[1]);
+      if constexpr (NCH == 2)
+        tc2_mma_chunk<C>(tbase, bh, bl, idesc, KC, KT, C::COL_AL2, C::COL_DC, false, &bar[1]);
+      else
+        tc2_mma_chunk<C>(tbase, bh, bl, idesc, 0, KT, C::COL_AL, C::COL_D, true, &bar[1]);
       arm(1, mma_phase);
       // the tile buffer has been consumed: the next tile's copies overlap
       // this chunk's MMAs and the epilogue
@@ -541,22 +558,31 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
       const float dte = dt * sGT[(D * D + D) * (ET + 1) + e];
       float* kr = sK + (size_t)(q * ET + e) * NP;
       constexpr int NCHK = (NN / 4 + NPART - 1) / NPART;
-      uint32_t dr[NCHK][4];
+      uint32_t dr[NCHK][4], dc[NCHK][4];
 #pragma unroll
       for (int t = 0; t < NCHK; ++t) {
         const int c4 = part + t * NPART;
-        if (c4 * 4 < NP) tmem_ld4_async(trow + C::COL_D + c4 * 4, dr[t]);  // warp-uniform condition
+        if (c4 * 4 < NP) {  // warp-uniform condition
+          tmem_ld4_async(trow + C::COL_D + c4 * 4, dr[t]);
+          if constexpr (NCH == 2) tmem_ld4_async(trow + C::COL_DC + c4 * 4, dc[t]);
+        }
       }
 #pragma unroll
       for (int t = 0; t < NCHK; ++t)
-        if ((part + t * NPART) * 4 < NP) tmem_wait_ld4(dr[t]);
+        if ((part + t * NPART) * 4 < NP) {
+          tmem_wait_ld4(dr[t]);
+          if constexpr (NCH == 2) tmem_wait_ld4(dc[t]);
+        }
 #pragma unroll
       for (int t = 0; t < NCHK; ++t) {
         const int i0 = (part + t * NPART) * 4;
         if (i0 >= NP) break;  // warp-uniform
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (i0 + u < NP) kr[i0 + u] = dte * __uint_as_float(dr[t][u]);
+        for (int u = 0; u < 4; ++u) {
+          float x = __uint_as_float(dr[t][u]);
+          if constexpr (NCH == 2) x += __uint_as_float(dc[t][u]);
+          if (i0 + u < NP) kr[i0 + u] = dte * x;
+        }
       }
     }
     tc_fence_before();
