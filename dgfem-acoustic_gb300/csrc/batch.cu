@@ -343,22 +343,13 @@ int dg_batch_create(int n, const dg_mesh_desc* meshes, const dg_phys* phys, cons
   if (b->fused_ok) {
     const int bps = dgk::stage_multi_blocks_per_sm();
     int64_t tiles = 0;
-    for (auto& g : b->groups) tiles += g.ctx->Epad / dgk::stage_multi_elems_per_tile(g.order);
-    b->fused_grid = (int)std::min<int64_t>(tiles, (int64_t)bps * b->groups[0].ctx->num_sms);
-    // every order's residual partial-sum array holds one row per block of the
-    // launch: grown where the group's own kernels need fewer rows
-    bool grown = true;
-    for (auto& g : b->groups)
-      if (b->fused_grid > g.ctx->max_grid) {
-        double* p = nullptr;
-        if (dgc::dev_alloc(g.ctx, (void**)&p, (size_t)b->fused_grid * 5 * sizeof(double)) != cudaSuccess) {
-          grown = false;
-          break;
-        }
-        g.ctx->partials = p;
-        g.ctx->max_grid = b->fused_grid;
-      }
-    if (!grown || bps <= 0 || b->fused_grid <= 0 || cudaMalloc(&b->d_queue, 4 * sizeof(unsigned)) != cudaSuccess) {
+    int cap = 1 << 30;
+    for (auto& g : b->groups) {
+      tiles += g.ctx->Epad / dgk::stage_multi_elems_per_tile(g.order);
+      cap = std::min(cap, g.ctx->max_grid);  // rows of every order's partial-sum array
+    }
+    b->fused_grid = (int)std::min<int64_t>(std::min<int64_t>(tiles, (int64_t)bps * b->groups[0].ctx->num_sms), cap);
+    if (bps <= 0 || b->fused_grid <= 0 || cudaMalloc(&b->d_queue, 4 * sizeof(unsigned)) != cudaSuccess) {
       cudaGetLastError();
       b->fused_ok = false;
     }

@@ -359,100 +359,13 @@ struct Pipe {
   static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
 };
 
-// The RK update of one tile (elements e0 .., C's shape, FP32) from dt*L in
-// sK [NV][ET][NP], by the nthr threads of the block (thread t) in one
-// coalesced float4 pass: the operands of two items (u, accumulator,
-// snapshot or stage input from global memory) are loaded before either
-// update is computed and stored, so that their loads are in flight
-// together.
-template <class C>
-__device__ __forceinline__ void tile_rk_update(const StageArgs<float>& a, const float* sK, int64_t e0, int t, int nthr,
-                                               ResAcc<float>& racc) {
-  constexpr int NP = C::NP, ET = C::ET, SEG4 = ET * NP / 4, TILE4 = C::NV * SEG4;
-  static_assert((ET * NP) % 4 == 0, "tile segments must be float4 multiples");
-  const int stage = a.stage;
-  const bool ld_y = stage == 1 || stage == 5, ld_ua = stage >= 2 && stage <= 4, ld_s = stage == 4;
-  for (int w0 = t; w0 < TILE4; w0 += 2 * nthr) {
-    float4 kv[2], x0[2], x1[2], x2[2];
-    int64_t gi[2];
-    int qv[2];
-    bool in[2];
-#pragma unroll
-    for (int g = 0; g < 2; ++g) {
-      const int w = w0 + g * nthr;
-      in[g] = w < TILE4;
-      const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
-      qv[g] = qq;
-      gi[g] = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
-      kv[g] = x0[g] = x1[g] = x2[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (in[g]) {
-        kv[g] = *reinterpret_cast<const float4*>(sK + (size_t)qq * ET * NP + r4 * 4);
-        if (ld_y) x0[g] = *reinterpret_cast<const float4*>(a.y_in + gi[g]);
-        if (ld_ua) {
-          x0[g] = *reinterpret_cast<const float4*>(a.u + gi[g]);
-          x1[g] = *reinterpret_cast<const float4*>(a.acc + gi[g]);
-        }
-        if (ld_s) x2[g] = *reinterpret_cast<const float4*>(a.snap + gi[g]);
-      }
-    }
-#pragma unroll
-    for (int g = 0; g < 2; ++g) {
-      if (!in[g]) continue;
-      const float4 v = kv[g];
-      switch (stage) {
-        case 0:
-          *reinterpret_cast<float4*>(a.k_out + gi[g]) = v;
-          break;
-        case 1: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.acc + gi[g]) = v;
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(y.x + 0.5f * v.x, y.y + 0.5f * v.y, y.z + 0.5f * v.z, y.w + 0.5f * v.w);
-          break;
-        }
-        case 2:
-        case 3: {
-          const float4 u = x0[g], ac = x1[g];
-          const float c = stage == 2 ? 0.5f : 1.0f;
-          *reinterpret_cast<float4*>(a.acc + gi[g]) =
-              make_float4(ac.x + 2.f * v.x, ac.y + 2.f * v.y, ac.z + 2.f * v.z, ac.w + 2.f * v.w);
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(u.x + c * v.x, u.y + c * v.y, u.z + c * v.z, u.w + c * v.w);
-          break;
-        }
-        case 4: {
-          const float4 u = x0[g], ac = x1[g], sn = x2[g];
-          const float4 un = make_float4(u.x + rk4_sixth(ac.x + v.x), u.y + rk4_sixth(ac.y + v.y),
-                                        u.z + rk4_sixth(ac.z + v.z), u.w + rk4_sixth(ac.w + v.w));
-          *reinterpret_cast<float4*>(a.u + gi[g]) = un;
-          racc.add(qv[g], sn.x, un.x, a.c0sq);
-          racc.add(qv[g], sn.y, un.y, a.c0sq);
-          racc.add(qv[g], sn.z, un.z, a.c0sq);
-          racc.add(qv[g], sn.w, un.w, a.c0sq);
-          break;
-        }
-        default: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) = make_float4(y.x + v.x, y.y + v.y, y.z + v.z, y.w + v.w);
-          break;
-        }
-      }
-    }
-  }
-}
-
 // One tile of the pipelined stage for elements e0 .. e0+ET-1: neighbour
 // gathers, volume term, face fluxes, lift and the RK update. The tile's stage
 // input and geometry records (sY, sGF, sGI) have arrived; its RK operands sE
 // (u, accumulator, snapshot: nepi of them) arrive on bar_epi with phase parity
 // epi_parity. sD holds Dt, sL the negated LIFT table. The caller
 // synchronises the block before the buffers are reused.
-// With STAGED false (the mixed-order kernel, FP32) the RK operands are not
-// staged: sE and bar_epi are unused, dt*L of the tile goes to sN once every
-// thread's lift has read it, and the whole block updates the tile in one
-// coalesced pass from global memory (tile_rk_update); the caller has
-// prefetched the tile's RK operands to L2.
-template <class C, typename T, bool STAGED = true>
+template <class C, typename T>
 __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* sY, const T* sGF, const int* sGI,
                                           const T* sE, T* sN, const T* sD, const T* sL, const short* sFm,
                                           const short* sNb, uint64_t* bar_epi, uint32_t epi_parity, int nepi, int tid,
@@ -630,20 +543,6 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
   }
 
   if (active) curved_override<T, NC, NV, NP>(a, e0 + e, i0, Lv);
-  if constexpr (!STAGED) {
-    __syncthreads();  // every lift has read the face fluxes in sN
-    if (active) {
-      const T dte = dt * sGF[e * RECF + C::S::PHYS_OFF + D];
-#pragma unroll
-      for (int q = 0; q < NV; ++q)
-#pragma unroll
-        for (int ii = 0; ii < NC; ++ii)
-          if (i0 + ii < NP) sN[(q * ET + e) * NP + i0 + ii] = dte * Lv[ii][q];
-    }
-    __syncthreads();
-    tile_rk_update<C>(a, sN, e0, tid, (int)blockDim.x, racc);
-    return;
-  }
   // ---- RK update from registers (vectorised when the node chunk allows) ----
   if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity, a.wait_limit)) ok = false;
   // after a timeout the operand buffer may still be landing: no RK update

@@ -14,13 +14,10 @@
 // Every order's reference operators sit in shared memory. The tile buffers
 // are two fixed slots sized for the largest order (consecutive queue items
 // may be of different orders; the next item's stage input and geometry
-// arrive by TMA while the current one computes), then the face-flux buffer,
-// also sized for the largest order. The RK operands are not staged: at the
-// end of a tile dt*L goes to the face buffer and the whole block updates the
-// tile in one coalesced pass from global memory (prefetched to L2 when the
-// item starts; pipe_tile with STAGED false). Every wait is bounded; after a
-// timeout a block records the error, drains its own copies (bounded) and
-// stops taking work.
+// arrive by TMA while the current one computes), then the RK operand and
+// face-flux buffers, also sized for the largest order. Every wait is
+// bounded; after a timeout a block records the error, drains its own copies
+// (bounded) and stops taking work.
 #pragma once
 #include <cstdint>
 
@@ -32,9 +29,8 @@ using MultiC2 = Pipe<float, 2, 2, 3, 64>;
 using MultiC3 = Pipe<float, 2, 3, 2, 32>;
 using MultiC4 = Pipe<float, 2, 4, 5, 32>;
 constexpr int kMultiNT = 160;
-// blocks per SM the register budget is set for (the shared memory allows
-// six; with the register cap of six blocks the per-tile code spills)
-constexpr int kMultiMinBlocks = 5;
+// blocks per SM the register budget is set for (the shared memory's limit)
+constexpr int kMultiMinBlocks = 4;
 
 template <typename A, typename B>
 constexpr A cmax(A x, B y) {
@@ -51,6 +47,10 @@ constexpr size_t multi_slot_bytes() {
   return RoundUp<C::NV * C::YSEG + C::GFB + C::GIB, 128>::v;
 }
 template <class C>
+constexpr size_t multi_epi_bytes() {
+  return 3 * (size_t)C::NV * C::YSEG;
+}
+template <class C>
 constexpr size_t multi_nbuf_bytes() {
   return C::SN_WORDS * 4;
 }
@@ -65,7 +65,8 @@ struct MultiLayout {
       cmax(cmax(multi_slot_bytes<MultiC2>(), multi_slot_bytes<MultiC3>()), multi_slot_bytes<MultiC4>());
   static constexpr size_t oSlot = RoundUp<oOps4 + multi_ops_bytes<MultiC4>(), 128>::v;  // 2 slots
   static constexpr size_t oE = oSlot + 2 * SLOT;
-  static constexpr size_t EPI = 0;  // RK operands are read from global memory (tile_rk_update)
+  static constexpr size_t EPI =
+      cmax(cmax(multi_epi_bytes<MultiC2>(), multi_epi_bytes<MultiC3>()), multi_epi_bytes<MultiC4>());
   static constexpr size_t oN = RoundUp<oE + EPI, 128>::v;
   static constexpr size_t NBUF =
       cmax(cmax(multi_nbuf_bytes<MultiC2>(), multi_nbuf_bytes<MultiC3>()), multi_nbuf_bytes<MultiC4>());
@@ -73,10 +74,6 @@ struct MultiLayout {
   static constexpr size_t bytes = oR + (size_t)(kMultiNT / 32) * 5 * sizeof(double);
 };
 
-static_assert(MultiC2::NV * MultiC2::ET * MultiC2::NP <= MultiC2::SN_WORDS &&
-                  MultiC3::NV * MultiC3::ET * MultiC3::NP <= MultiC3::SN_WORDS &&
-                  MultiC4::NV * MultiC4::ET * MultiC4::NP <= MultiC4::SN_WORDS,
-              "dt*L of a tile must fit in its face buffer");
 static_assert(MultiC2::NT <= kMultiNT && MultiC3::NT <= kMultiNT && MultiC4::NT <= kMultiNT,
               "the block holds every order's tile shape");
 static_assert(kMultiNT % 32 == 0 && MultiC2::NT % 32 == 0 && MultiC3::NT % 32 == 0 && MultiC4::NT % 32 == 0,
@@ -141,12 +138,18 @@ __device__ __forceinline__ void multi_issue_tile(const StageArgs<float>& a, int 
   tma_load_1d(sGI, a.geoI + e0 * RECI, C::GIB, bar);
 }
 
-// L2 prefetch of RK operand k (0 u, 1 accumulator, 2 snapshot) of variable
-// q of a tile of order C.
 template <class C>
-__device__ __forceinline__ void multi_prefetch_epi(const StageArgs<float>& a, int tile, int k, int q) {
-  const float* src = k == 0 ? a.u : (k == 1 ? a.acc : a.snap);
-  if (q < C::NV) prefetch_l2(src + q * a.stride + (int64_t)tile * C::ET * C::NP, C::YSEG);
+__device__ __forceinline__ void multi_issue_epi(const StageArgs<float>& a, int tile, float* sE, int nepi,
+                                                uint64_t* bar) {
+  constexpr int NV = C::NV, ET = C::ET, NP = C::NP;
+  const int64_t e0 = (int64_t)tile * ET;
+  mbar_expect_tx(bar, nepi * NV * C::YSEG);
+  for (int k = 0; k < nepi; ++k) {
+    const float* src = k == 0 ? a.u : (k == 1 ? a.acc : a.snap);
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      tma_load_1d(sE + ((size_t)k * NV + q) * ET * NP, src + q * a.stride + e0 * NP, C::YSEG, bar);
+  }
 }
 
 template <class C>
@@ -157,8 +160,8 @@ __device__ __forceinline__ void multi_run_tile(const StageArgs<float>& a, int ti
   float* sY = reinterpret_cast<float*>(slot);
   const float* sGF = reinterpret_cast<const float*>(slot + C::NV * C::YSEG);
   const int* sGI = reinterpret_cast<const int*>(slot + C::NV * C::YSEG + C::GFB);
-  pipe_tile<C, float, false>(a, (int64_t)tile * C::ET, sY, sGF, sGI, sE, sN, o.sD, o.sL, o.sFm, o.sNb, bar_epi,
-                             epi_parity, nepi, tid, ok, racc);
+  pipe_tile<C, float>(a, (int64_t)tile * C::ET, sY, sGF, sGI, sE, sN, o.sD, o.sL, o.sFm, o.sNb, bar_epi, epi_parity,
+                      nepi, tid, ok, racc);
 }
 
 __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(const MultiArgs m, int* err) {
@@ -261,14 +264,12 @@ __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(
         issue(next, b ^ 1), pend |= 1u << (b ^ 1);
         ahead = (int)atomicAdd(m.queue, 1u);
       }
-    }
-    // this item's RK operands towards L2 (read by the coalesced RK update at
-    // the end of the tile)
-    if (tid < 3 * nepi) {
-      const int k = tid / 3, q = tid - (tid / 3) * 3;
-      if (g == 0) multi_prefetch_epi<MultiC2>(m.g[0], tile, k, q);
-      if (g == 1) multi_prefetch_epi<MultiC3>(m.g[1], tile, k, q);
-      if (g == 2) multi_prefetch_epi<MultiC4>(m.g[2], tile, k, q);
+      if (nepi > 0) {
+        pend |= 4u;
+        if (g == 0) multi_issue_epi<MultiC2>(m.g[0], tile, sE, nepi, &bar[2]);
+        if (g == 1) multi_issue_epi<MultiC3>(m.g[1], tile, sE, nepi, &bar[2]);
+        if (g == 2) multi_issue_epi<MultiC4>(m.g[2], tile, sE, nepi, &bar[2]);
+      }
     }
     unsigned char* slot = slots + (size_t)b * L::SLOT;
     if (g == 0)
@@ -277,7 +278,8 @@ __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(
       multi_run_tile<MultiC3>(m.g[1], tile, slot, sE, sN, ops3, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
     else
       multi_run_tile<MultiC4>(m.g[2], tile, slot, sE, sN, ops4, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
-    if (__syncthreads_or(!ok)) {  // buffers of this item are free again
+    if (tid == 0 && ok) pend &= ~4u;  // the RK operands arrived (waited inside the tile)
+    if (__syncthreads_or(!ok)) {      // buffers of this item are free again
       ok = false;
       break;
     }
@@ -286,6 +288,7 @@ __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(
     // after a timeout: bounded waits for this block's copies still in flight
     for (int i = 0; i < 2; ++i)
       if (pend & (1u << i)) mbar_wait(&bar[i], (uint32_t)(((it + (i != (it & 1))) >> 1) & 1));
+    if (pend & 4u) mbar_wait(&bar[2], (uint32_t)(it & 1));
     if (!ok) atomicOr(err, 1);
   }
 
