@@ -278,9 +278,14 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
                  : dgk::launch_stage_tc(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
   }
-  if (c->variant >= dgk::kStage3Variant) {
+  if (dgk::is_stage3_variant(c->variant)) {
     if constexpr (sizeof(T) == 4)
       return dgk::launch_stage3(c->dim, c->order, c->variant - dgk::kStage3Variant, a, c->grid2, c->d_err, c->stream);
+    return cudaErrorInvalidValue;
+  }
+  if (dgk::is_wide_variant(c->variant)) {
+    if constexpr (sizeof(T) == 4)
+      return dgk::launch_stage4(c->dim, c->order, c->variant - dgk::kWideVariant, a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
   }
   if (c->variant >= 0) {
@@ -460,16 +465,20 @@ void to_dev_ops(const dgref::RefElement& re, std::vector<T>& Dt, std::vector<T>&
 }
 
 
-// The tensor-core and constant-operator kernels have no curved-element
-// path; the baseline and pipelined kernels take the curved right-hand side.
+// The tensor-core, constant-operator and flux-form kernels have no
+// curved-element path; the baseline and pipelined kernels take the curved
+// right-hand side.
 bool variant_handles_mesh(const dg_ctx* c, int v) {
   return c->ncurved == 0 || !(dgk::is_tc_variant(v) || v >= dgk::kStage3Variant);
 }
 
 dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
-  if (v >= dgk::kStage3Variant)
-    return c->prec == DG_FP32 ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
+  if (dgk::is_wide_variant(v))
+    return c->prec == DG_FP32 ? dgk::stage4_info(c->dim, c->order, v - dgk::kWideVariant)
                               : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
+  if (v >= dgk::kStage3Variant)
+    return c->prec == DG_FP32 && dgk::is_stage3_variant(v) ? dgk::stage3_info(c->dim, c->order, v - dgk::kStage3Variant)
+                                                           : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (dgk::is_tc_variant(v))
     return c->prec != DG_FP32        ? dgk::Stage2Info{0, 0, 0, 0, 0, 0}
            : dgk::is_tc2_variant(v) ? dgk::stage_tc2_info(c->dim, c->order, dgk::tc_npart(v))
@@ -485,7 +494,8 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
 // kTcVariant .. kTcVariant + 4 the tensor-core kernels, kStage3Variant + k
-// constant-operator variant k (all three FP32).
+// constant-operator variant k, kWideVariant + k flux-form variant k (the
+// last three FP32).
 bool set_variant(dg_ctx* c, int v) {
   if (v < 0) {
     c->variant = -1;
@@ -494,7 +504,7 @@ bool set_variant(dg_ctx* c, int v) {
   if (!variant_handles_mesh(c, v)) return false;
   dgk::Stage2Info si = stage2_info(c, v);
   if (si.nc == 0 || si.blocks_per_sm <= 0 || c->Epad % si.et != 0) return false;
-  if (v >= dgk::kStage3Variant) {
+  if (dgk::is_stage3_variant(v)) {
     // the constant-operator kernels read Dt [r][i][j] and LIFT [k][i] from
     // constant memory (uploaded once per device and element type)
     const int np = c->re.np, D = c->re.dim, nk = c->re.nf * c->re.nfp;
@@ -622,6 +632,11 @@ int select_variant(dg_ctx* c, int want) {
     dgk::Stage2Info si = stage2_info(c, dgk::kStage3Variant + k);
     if (si.nc == 0) break;
     if (si.blocks_per_sm > 0) cands.push_back(dgk::kStage3Variant + k);
+  }
+  for (int k = 0; k < 16; ++k) {
+    dgk::Stage2Info si = stage2_info(c, dgk::kWideVariant + k);
+    if (si.nc == 0) break;
+    if (si.blocks_per_sm > 0) cands.push_back(dgk::kWideVariant + k);
   }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -899,6 +914,11 @@ int dgc::create_ctx(const dg_mesh_desc* mesh, const dg_phys* phys, int precision
   }
   for (int k = 0; k < 8; ++k) {
     dgk::Stage2Info si = stage2_info(c, dgk::kStage3Variant + k);
+    if (si.nc == 0) break;
+    c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
+  }
+  for (int k = 0; k < 16; ++k) {
+    dgk::Stage2Info si = stage2_info(c, dgk::kWideVariant + k);
     if (si.nc == 0) break;
     c->max_grid = std::max<int>(c->max_grid, (int)std::min<int64_t>(c->Epad / si.et, (int64_t)si.blocks_per_sm * c->num_sms));
   }

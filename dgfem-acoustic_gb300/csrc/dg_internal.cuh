@@ -220,6 +220,14 @@ cudaError_t stage3_upload_ops(int dim, int order, const float* Dt, const float* 
 cudaError_t launch_stage3(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,
                           cudaStream_t s);
 Stage2Info stage3_info(int dim, int order, int variant);
+// Flux-form stage kernel (stage4.cuh, FP32 state, triangles): variant ids
+// kWideVariant + k of the context's kernel selection.
+constexpr int kWideVariant = 48;
+inline bool is_stage3_variant(int v) { return v >= kStage3Variant && v < kWideVariant; }
+inline bool is_wide_variant(int v) { return v >= kWideVariant && v < kWideVariant + 16; }
+cudaError_t launch_stage4(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,
+                          cudaStream_t s);
+Stage2Info stage4_info(int dim, int order, int variant);
 // Mixed-order stage kernel of the batched ensemble (stage_multi.cuh): 2-D,
 // FP32, orders 2-4, one launch per RK stage over every order's tiles.
 // Per-launch description: one StageArgs per order slot (slot k holds order

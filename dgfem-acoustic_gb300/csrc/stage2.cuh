@@ -319,6 +319,7 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
 template <typename T, int D_, int P, int NC_, int ET_>
 struct Pipe {
   using S = ShapeT<D_, P, T>;
+  static constexpr bool kStaged = true;  // RK operands staged in shared memory by TMA
   static constexpr int D = D_;
   static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NV = S::NV, NPERM = S::NPERM, NK = NF * NFP;
   static constexpr int NC = NC_;
@@ -359,6 +360,77 @@ struct Pipe {
   static_assert((ET * NP * sizeof(T)) % 16 == 0, "tile segments must be 16-byte multiples");
 };
 
+// RK update of this thread's chunk of output nodes (i0 .. i0+NC of element
+// e0 + e, every variable) from the operator result Lv in registers: stage 0
+// writes dt*L; RK4 stages 1-3 write the accumulator and the next stage input;
+// stage 4 writes the new state and adds to the residual sums; stage 5
+// (Euler) writes u + dt*L. The tile's u (eu), accumulator and snapshot (in sE
+// after eu's slot) are in shared memory in the [q][e][i] layout; dte is dt
+// times the element's step scale. Global stores are VW-wide vectors (the
+// chunk and element starts must be VW-aligned, NP a multiple of VW).
+template <typename T, int NC, int NV, int VW, int ET, int NP>
+__device__ __forceinline__ void rk_update_regs(const StageArgs<T>& a, int64_t e0, int e, int i0, const T (&Lv)[NC][NV],
+                                               const T* eu, const T* sE, T dte, ResAcc<T>& racc) {
+  const int64_t stride = a.stride;
+  const T* ea = sE + (size_t)NV * ET * NP;
+  const T* es = sE + (size_t)2 * NV * ET * NP;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+#pragma unroll
+    for (int c0 = 0; c0 < NC; c0 += VW) {
+      const int i = i0 + c0;
+      if (i >= NP) continue;
+      const int lidx = (q * ET + e) * NP + i;
+      const int64_t g = q * stride + (e0 + e) * NP + i;
+      T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
+#pragma unroll
+      for (int v = 0; v < VW; ++v) kv[v] = dte * Lv[c0 + v][q];
+      switch (a.stage) {
+        case 0:
+          vstore<T, VW>(a.k_out + g, kv);
+          break;
+        case 1:
+          vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) o1[v] = kv[v], o2[v] = xu[v] + (T)0.5 * kv[v];
+          vstore<T, VW>(a.acc + g, o1);
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+        case 2:
+        case 3:
+          vload<T, VW>(xu, eu + lidx);
+          vload<T, VW>(xa, ea + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v)
+            o1[v] = xa[v] + (T)2 * kv[v], o2[v] = xu[v] + (a.stage == 2 ? (T)0.5 * kv[v] : kv[v]);
+          vstore<T, VW>(a.acc + g, o1);
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+        case 4: {
+          T xs[VW];
+          vload<T, VW>(xu, eu + lidx);
+          vload<T, VW>(xa, ea + lidx);
+          vload<T, VW>(xs, es + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) {
+            const T un = xu[v] + rk4_sixth(xa[v] + kv[v]);
+            o1[v] = un;
+            racc.add(q, xs[v], un, a.c0sq);
+          }
+          vstore<T, VW>(a.u + g, o1);
+          break;
+        }
+        default:
+          vload<T, VW>(xu, eu + lidx);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) o2[v] = xu[v] + kv[v];
+          vstore<T, VW>(a.y_out + g, o2);
+          break;
+      }
+    }
+  }
+}
+
 // One tile of the pipelined stage for elements e0 .. e0+ET-1: neighbour
 // gathers, volume term, face fluxes, lift and the RK update. The tile's stage
 // input and geometry records (sY, sGF, sGI) have arrived; its RK operands sE
@@ -372,7 +444,6 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
                                           bool& ok, ResAcc<T>& racc) {
   constexpr int D = C::D, NP = C::NP, NV = C::NV, NK = C::NK;
   constexpr int NC = C::NC, NSPLIT = C::NSPLIT, ET = C::ET, RECF = C::RECF;
-  const int stage = a.stage;
   const int64_t stride = a.stride;
   const T rhoc2 = (T)a.ph.rhoc2, inv_rho0 = (T)a.ph.inv_rho0, half_c0 = (T)a.ph.half_c0;
   const T dt = (T)a.dt;
@@ -547,74 +618,33 @@ __device__ __forceinline__ void pipe_tile(const StageArgs<T>& a, int64_t e0, T* 
   if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity, a.wait_limit)) ok = false;
   // after a timeout the operand buffer may still be landing: no RK update
   if (!active || !ok) return;
-  const T* eu = (nepi > 0) ? sE : sY;  // u of this tile (stage input when u == y_in)
-  const T* ea = sE + (size_t)NV * ET * NP;
-  const T* es = sE + (size_t)2 * NV * ET * NP;
-  constexpr int VW = C::VW;
-  const T dte = dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
-#pragma unroll
-  for (int q = 0; q < NV; ++q) {
-#pragma unroll
-    for (int c0 = 0; c0 < NC; c0 += VW) {
-      const int i = i0 + c0;
-      if (i >= NP) continue;
-      const int lidx = (q * ET + e) * NP + i;
-      const int64_t g = q * stride + (e0 + e) * NP + i;
-      T kv[VW], o1[VW], o2[VW], xu[VW], xa[VW];
-#pragma unroll
-      for (int v = 0; v < VW; ++v) kv[v] = dte * Lv[c0 + v][q];
-      switch (stage) {
-        case 0:
-          vstore<T, VW>(a.k_out + g, kv);
-          break;
-        case 1:
-          vload<T, VW>(xu, eu + lidx);
-#pragma unroll
-          for (int v = 0; v < VW; ++v) o1[v] = kv[v], o2[v] = xu[v] + (T)0.5 * kv[v];
-          vstore<T, VW>(a.acc + g, o1);
-          vstore<T, VW>(a.y_out + g, o2);
-          break;
-        case 2:
-        case 3:
-          vload<T, VW>(xu, eu + lidx);
-          vload<T, VW>(xa, ea + lidx);
-#pragma unroll
-          for (int v = 0; v < VW; ++v)
-            o1[v] = xa[v] + (T)2 * kv[v], o2[v] = xu[v] + (stage == 2 ? (T)0.5 * kv[v] : kv[v]);
-          vstore<T, VW>(a.acc + g, o1);
-          vstore<T, VW>(a.y_out + g, o2);
-          break;
-        case 4: {
-          T xs[VW];
-          vload<T, VW>(xu, eu + lidx);
-          vload<T, VW>(xa, ea + lidx);
-          vload<T, VW>(xs, es + lidx);
-#pragma unroll
-          for (int v = 0; v < VW; ++v) {
-            const T un = xu[v] + rk4_sixth(xa[v] + kv[v]);
-            o1[v] = un;
-            racc.add(q, xs[v], un, a.c0sq);
-          }
-          vstore<T, VW>(a.u + g, o1);
-          break;
-        }
-        default:
-          vload<T, VW>(xu, eu + lidx);
-#pragma unroll
-          for (int v = 0; v < VW; ++v) o2[v] = xu[v] + kv[v];
-          vstore<T, VW>(a.y_out + g, o2);
-          break;
-      }
-    }
-  }
+  rk_update_regs<T, NC, NV, C::VW, ET, NP>(a, e0, e, i0, Lv, (nepi > 0) ? sE : sY, sE,
+                                           dt * sGF[e * RECF + C::S::PHYS_OFF + D], racc);
 }
 
-template <typename T, int D, int P, int NC_, int ET_>
-__global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(const StageArgs<T> a, int* err) {
-  using C = Pipe<T, D, P, NC_, ET_>;
+// Operator tables and tile body of the pipelined kernel: Dt [D][NP j][NP i]
+// and the negated LIFT [NK][NP i] in shared memory, pipe_tile per tile.
+struct PipeTileOps {
+  template <class C, typename T>
+  __device__ static void load_ops(T* sD, T* sL, const StageArgs<T>& a, int tid) {
+    for (int i = tid; i < C::D * C::NP * C::NP; i += C::NT) sD[i] = a.Dt[i];
+    for (int i = tid; i < C::NK * C::NP; i += C::NT) sL[i] = -a.LIFT[i];  // negated for pipe_tile's lift
+  }
+  template <class C, typename T>
+  __device__ static void run(const StageArgs<T>& a, int64_t e0, T* sY, const T* sGF, const int* sGI, const T* sE,
+                             T* sN, const T* sD, const T* sL, const short* sFm, const short* sNb, uint64_t* bar_epi,
+                             uint32_t epi_parity, int nepi, int tid, bool& ok, ResAcc<T>& racc) {
+    pipe_tile<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, bar_epi, epi_parity, nepi, tid, ok, racc);
+  }
+};
+
+// The persistent tile loop of the pipelined kernels: C gives the shape and
+// the shared-memory layout (oBar, oD, oL, oFm, oNb, oY, oGF, oGI, oE, oN,
+// oR), Ops the operator tables and the per-tile body.
+template <class C, typename T, class Ops>
+__device__ __forceinline__ void pipe_loop(const StageArgs<T>& a, int* err, unsigned char* sm) {
   constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
   constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, RECI = C::RECI;
-  extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::oBar);  // [0],[1]: tile buffers, [2]: epilogue operands
   T* sD = reinterpret_cast<T*>(sm + C::oD);
   T* sL = reinterpret_cast<T*>(sm + C::oL);
@@ -659,8 +689,7 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
     mbar_init(&bar[2], 1);
     fence_mbar_init();
   }
-  for (int i = tid; i < D * NP * NP; i += NT) sD[i] = a.Dt[i];
-  for (int i = tid; i < NK * NP; i += NT) sL[i] = -a.LIFT[i];  // negated for pipe_tile's lift
+  Ops::template load_ops<C, T>(sD, sL, a, tid);
   for (int i = tid; i < NK; i += NT) sFm[i] = a.fmask[i];
   for (int i = tid; i < NF * NPERM * NFP; i += NT) sNb[i] = a.nbrnode[i];
   __syncthreads();
@@ -694,9 +723,10 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       fence_proxy_async();
       const int nt = tile + gridDim.x;
       if (nt < a.ntiles) issue_tile(nt, b ^ 1), arm(b ^ 1, (it + 1) >> 1);
-      if (nepi > 0) issue_epi(tile), arm(2, it);
+      if (C::kStaged && nepi > 0) issue_epi(tile), arm(2, it);
     }
-    pipe_tile<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, &bar[2], (uint32_t)(it & 1), nepi, tid, ok, racc);
+    Ops::template run<C, T>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, &bar[2], (uint32_t)(it & 1), nepi, tid, ok,
+                            racc);
     if (tid == 0 && ok) pend &= ~4u;  // thread 0 observed the operand copies (inside the tile)
     if (__syncthreads_or(!ok)) {      // buffers of this tile are free again
       ok = false;
@@ -726,6 +756,13 @@ __global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(con
       a.partials[blockIdx.x * 5 + tid] = v;
     }
   }
+}
+
+
+template <typename T, int D, int P, int NC_, int ET_>
+__global__ void __launch_bounds__(Pipe<T, D, P, NC_, ET_>::NT) stage2_kernel(const StageArgs<T> a, int* err) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  pipe_loop<Pipe<T, D, P, NC_, ET_>, T, PipeTileOps>(a, err, sm);
 }
 
 template <typename T, int D, int P, int NC_, int ET_>

@@ -30,9 +30,10 @@ def _mesh(pkg, dim, p, reflect=True):
 
 def kernel_variants(pkg, S):
     """-1 (baseline kernel) and every other stage-kernel variant available
-    for S: pipelined (0..), tensor-core (16-18), constant-operator (32..)."""
+    for S: pipelined (0..), tensor-core (16-20), constant-operator (32..),
+    flux-form (48..)."""
     out = [-1]
-    for v in list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)):
+    for v in list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)) + list(range(48, 64)):
         if S.kernel_info(v)[0] > 0:
             out.append(v)
     return out
@@ -93,7 +94,7 @@ def _sources_observers(mesh, srcs, obs):
     return sdofs, odofs, ows
 
 
-@pytest.mark.parametrize("variant", [-1, 0, 1, 32, 33])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 32, 33, 48, 49, 50, 51, 52, 53])
 @pytest.mark.parametrize("dim,p,prec", [(2, 3, "fp64"), (3, 2, "fp64"), (3, 3, "fp64"), (2, 3, "fp32"), (3, 3, "fp32"),
                                         (2, 4, "fp32"), (2, 2, "fp32")])
 def test_run_parity(pkg, oracle, dim, p, prec, variant):
