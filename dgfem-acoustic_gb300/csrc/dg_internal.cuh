@@ -220,7 +220,7 @@ cudaError_t stage3_upload_ops(int dim, int order, const float* Dt, const float* 
 cudaError_t launch_stage3(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,
                           cudaStream_t s);
 Stage2Info stage3_info(int dim, int order, int variant);
-// Flux-form stage kernel (stage4.cuh, FP32 state, triangles): variant ids
+// Wide-chunk stage kernel (stage4.cuh, FP32 state): variant ids
 // kWideVariant + k of the context's kernel selection.
 constexpr int kWideVariant = 48;
 inline bool is_stage3_variant(int v) { return v >= kStage3Variant && v < kWideVariant; }

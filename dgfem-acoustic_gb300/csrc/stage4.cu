@@ -1,5 +1,5 @@
 // Instantiations of the wide-chunk stage kernel (stage4.cuh; FP32 state,
-// triangles of orders 1..4). Variants (nodes per thread NC, elements per
+// triangles of orders 1..4, tetrahedra of orders 3 and 4). Variants (nodes per thread NC, elements per
 // tile ET, volume form, operand staging) are offered to the context's kernel
 // selection as kWideVariant + k.
 #include "stage4.cuh"
@@ -9,14 +9,16 @@ namespace dgk {
 namespace {
 // per (dim, order): candidate (NC, ET, volume form, operands staged)
 constexpr int F = kFluxForm, W = kWForm;
-#define DGK_S4_VARIANTS(X)                                                                          \
-  X(2, 1, 4, 128, W, false) X(2, 1, 4, 128, F, true)                                                \
-  X(2, 2, 6, 64, W, false) X(2, 2, 6, 64, F, false) X(2, 2, 6, 64, F, true) X(2, 2, 6, 128, W, false) \
-  X(2, 2, 4, 64, W, false)                                                                          \
-  X(2, 3, 6, 32, W, false) X(2, 3, 6, 32, F, false) X(2, 3, 6, 32, F, true) X(2, 3, 6, 64, W, false)  \
-  X(2, 3, 4, 32, W, false) X(2, 3, 10, 64, W, false)                                                \
-  X(2, 4, 8, 32, W, false) X(2, 4, 8, 32, F, false) X(2, 4, 8, 32, F, true) X(2, 4, 8, 64, W, false)  \
-  X(2, 4, 4, 32, W, false) X(2, 4, 6, 32, W, false)
+#define DGK_S4_VARIANTS(X)                                                                            \
+  X(2, 1, 4, 128, W, false) X(2, 1, 4, 128, F, true)                                                  \
+  X(2, 2, 6, 64, W, false) X(2, 2, 6, 64, F, false) X(2, 2, 6, 64, F, true) X(2, 2, 6, 128, W, false)   \
+  X(2, 2, 4, 64, W, false)                                                                            \
+  X(2, 3, 6, 32, W, false) X(2, 3, 6, 32, F, false) X(2, 3, 6, 32, F, true) X(2, 3, 6, 64, W, false)    \
+  X(2, 3, 4, 32, W, false) X(2, 3, 10, 64, W, false)                                                  \
+  X(2, 4, 8, 32, W, false) X(2, 4, 8, 32, F, false) X(2, 4, 8, 32, F, true) X(2, 4, 8, 64, W, false)    \
+  X(2, 4, 4, 32, W, false) X(2, 4, 6, 32, W, false)                                                   \
+  X(3, 3, 2, 32, W, false) X(3, 3, 4, 32, W, false) X(3, 3, 4, 32, F, false)                           \
+  X(3, 4, 6, 32, W, false) X(3, 4, 4, 32, W, false)
 }  // namespace
 
 cudaError_t launch_stage4(int dim, int order, int variant, const StageArgs<float>& a, int grid, int* err,

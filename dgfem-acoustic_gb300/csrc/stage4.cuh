@@ -1,4 +1,4 @@
-// Wide-chunk pipelined RK4 stage kernel (sm_103a, FP32 state, triangles).
+// Wide-chunk pipelined RK4 stage kernel (sm_103a, FP32 state).
 //
 // Same arithmetic as the reference's per-stage work (src/Mesh.cpp:734-975,
 // src/solver.cpp:38-57, :488-516) and the same tile pipeline as the

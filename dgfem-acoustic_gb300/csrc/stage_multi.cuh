@@ -4,33 +4,34 @@
 // The batch keeps one disjoint-union mesh per element order (batch.cu). This
 // kernel advances all of them in one launch: its blocks take tiles from a
 // work queue over every order's tiles (an atomic counter; order after order)
-// and run each tile with the pipelined kernel's per-tile code for that order
-// (pipe_tile in stage2.cuh) with that order's own tile shape, the shape of
-// its fastest pipelined variant; the block has the largest shape's thread
-// count (160) and the threads past a shape's count idle in its tiles:
-//   p = 2: 64 elements per tile, 3 nodes per thread, 128 threads;
-//   p = 3: 32 elements per tile, 2 nodes per thread, 160 threads;
-//   p = 4: 32 elements per tile, 5 nodes per thread, 96 threads.
-// Every order's reference operators sit in shared memory. The tile buffers
-// are two fixed slots sized for the largest order (consecutive queue items
-// may be of different orders; the next item's stage input and geometry
-// arrive by TMA while the current one computes), then the RK operand and
-// face-flux buffers, also sized for the largest order. Every wait is
-// bounded; after a timeout a block records the error, drains its own copies
-// (bounded) and stops taking work.
+// and run each tile with the wide-chunk kernel's per-tile code for that
+// order (wide_tile in stage4.cuh) with that order's own tile shape; the
+// block has the largest shape's thread count and the threads past a shape's
+// count idle in its tiles (the shapes below all have 64 threads):
+//   p = 2: 64 elements per tile, 6 nodes per thread, one thread per element;
+//   p = 3: 32 elements per tile, 6 nodes per thread, two per element;
+//   p = 4: 32 elements per tile, 8 nodes per thread, two per element;
+// all with the volume contraction per reference direction (W form) and the
+// RK operands read from L2 by the coalesced update (not staged). Every
+// order's reference operators sit in shared memory. The tile buffers are two
+// fixed slots sized for the largest order (consecutive queue items may be of
+// different orders; the next item's stage input and geometry arrive by TMA
+// while the current one computes), then the face-flux buffer, also sized for
+// the largest order. Every wait is bounded; after a timeout a block records
+// the error, drains its own copies (bounded) and stops taking work.
 #pragma once
 #include <cstdint>
 
-#include "stage2.cuh"
+#include "stage4.cuh"
 
 namespace dgk {
 
-using MultiC2 = Pipe<float, 2, 2, 3, 64>;
-using MultiC3 = Pipe<float, 2, 3, 2, 32>;
-using MultiC4 = Pipe<float, 2, 4, 5, 32>;
-constexpr int kMultiNT = 160;
+using MultiC2 = Wide<2, 2, 6, 64, kWForm, false>;
+using MultiC3 = Wide<2, 3, 6, 32, kWForm, false>;
+using MultiC4 = Wide<2, 4, 8, 32, kWForm, false>;
+constexpr int kMultiNT = 64;
 // blocks per SM the register budget is set for (the shared memory's limit)
-constexpr int kMultiMinBlocks = 4;
+constexpr int kMultiMinBlocks = 6;
 
 template <typename A, typename B>
 constexpr A cmax(A x, B y) {
@@ -48,7 +49,7 @@ constexpr size_t multi_slot_bytes() {
 }
 template <class C>
 constexpr size_t multi_epi_bytes() {
-  return 3 * (size_t)C::NV * C::YSEG;
+  return C::kStaged ? 3 * (size_t)C::NV * C::YSEG : 0;
 }
 template <class C>
 constexpr size_t multi_nbuf_bytes() {
@@ -96,13 +97,12 @@ struct OpsSm {
     return o;
   }
   __device__ static void load(unsigned char* base, const StageArgs<float>& a, int tid) {
-    constexpr int D = C::D, NP = C::NP, NK = C::NK, NF = C::NF, NFP = C::NFP, NPERM = C::NPERM;
+    constexpr int NK = C::NK, NF = C::NF, NFP = C::NFP, NPERM = C::NPERM;
     float* sD = reinterpret_cast<float*>(base);
     float* sL = reinterpret_cast<float*>(base + (C::oL - C::oD));
     short* sFm = reinterpret_cast<short*>(base + (C::oFm - C::oD));
     short* sNb = reinterpret_cast<short*>(base + (C::oNb - C::oD));
-    for (int i = tid; i < D * NP * NP; i += kMultiNT) sD[i] = a.Dt[i];
-    for (int i = tid; i < NK * NP; i += kMultiNT) sL[i] = -a.LIFT[i];  // negated for pipe_tile's lift
+    WideTileOps::load_ops<C, float>(sD, sL, a, tid, kMultiNT);
     for (int i = tid; i < NK; i += kMultiNT) sFm[i] = a.fmask[i];
     for (int i = tid; i < NF * NPERM * NFP; i += kMultiNT) sNb[i] = a.nbrnode[i];
   }
@@ -160,8 +160,8 @@ __device__ __forceinline__ void multi_run_tile(const StageArgs<float>& a, int ti
   float* sY = reinterpret_cast<float*>(slot);
   const float* sGF = reinterpret_cast<const float*>(slot + C::NV * C::YSEG);
   const int* sGI = reinterpret_cast<const int*>(slot + C::NV * C::YSEG + C::GFB);
-  pipe_tile<C, float>(a, (int64_t)tile * C::ET, sY, sGF, sGI, sE, sN, o.sD, o.sL, o.sFm, o.sNb, bar_epi, epi_parity,
-                      nepi, tid, ok, racc);
+  wide_tile<C>(a, (int64_t)tile * C::ET, sY, sGF, sGI, sE, sN, o.sD, o.sL, o.sFm, o.sNb, bar_epi, epi_parity, nepi,
+               tid, ok, racc);
 }
 
 __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(const MultiArgs m, int* err) {
@@ -265,10 +265,9 @@ __global__ void __launch_bounds__(kMultiNT, kMultiMinBlocks) stage_multi_kernel(
         ahead = (int)atomicAdd(m.queue, 1u);
       }
       if (nepi > 0) {
-        pend |= 4u;
-        if (g == 0) multi_issue_epi<MultiC2>(m.g[0], tile, sE, nepi, &bar[2]);
-        if (g == 1) multi_issue_epi<MultiC3>(m.g[1], tile, sE, nepi, &bar[2]);
-        if (g == 2) multi_issue_epi<MultiC4>(m.g[2], tile, sE, nepi, &bar[2]);
+        if (g == 0 && MultiC2::kStaged) multi_issue_epi<MultiC2>(m.g[0], tile, sE, nepi, &bar[2]), pend |= 4u;
+        if (g == 1 && MultiC3::kStaged) multi_issue_epi<MultiC3>(m.g[1], tile, sE, nepi, &bar[2]), pend |= 4u;
+        if (g == 2 && MultiC4::kStaged) multi_issue_epi<MultiC4>(m.g[2], tile, sE, nepi, &bar[2]), pend |= 4u;
       }
     }
     unsigned char* slot = slots + (size_t)b * L::SLOT;

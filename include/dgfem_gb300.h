@@ -270,13 +270,14 @@ int dg_batch_set_observers(dg_batch* b, int inst, int n_obs, const int64_t* offs
 int dg_batch_run(dg_batch* b, int64_t n_steps, double* obs);
 /* timed steps (CUDA events around each per-step graph launch) */
 int dg_batch_bench(dg_batch* b, int64_t n_steps, double* step_ms);
-/* A batch of FP32 2-D instances of orders 2-4 can run each RK stage of all
- * its instances as one persistent launch whose blocks take element tiles of
- * every order from a work queue (on = 1; also selected at creation by the
- * environment variable DGFEM_BATCH_FUSED=1); the default (on = 0) runs one
- * stage kernel per element order, as parallel branches of the step's graph.
- * Returns DG_ERR_ARG when on != 0 and the batch holds other element types or
- * FP64. */
+/* A batch of FP32 2-D straight-sided instances of orders 2-4 runs each RK
+ * stage of all its instances as one persistent launch whose blocks take
+ * element tiles of every order from a work queue (on = 1, the default for
+ * such a batch); on = 0 (also selected at creation by the environment
+ * variable DGFEM_BATCH_FUSED=0) runs one stage kernel per element order, as
+ * parallel branches of the step's graph, which is also what every other
+ * batch runs. Returns DG_ERR_ARG when on != 0 and the batch holds other
+ * element types or FP64. */
 int dg_batch_set_fused(dg_batch* b, int on);
 /* 1 when the batch runs one launch per stage for all orders, else 0 */
 int dg_batch_fused(const dg_batch* b);
