@@ -265,6 +265,8 @@ dgk::StageArgs<T> stage_args(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k
   a.dt = dt;
   a.c0sq = c->c0sq;
   a.ph = c->ph;
+  a.f_rhoc2 = (float)c->ph.rhoc2, a.f_inv_rho0 = (float)c->ph.inv_rho0, a.f_half_c0 = (float)c->ph.half_c0;
+  a.f_dt = (float)dt;
   return a;
 }
 

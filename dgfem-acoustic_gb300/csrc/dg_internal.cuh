@@ -146,6 +146,9 @@ struct StageArgs {
   double dt;
   double c0sq;
   Phys ph;
+  // FP32 copies of rho0 c0^2, 1/rho0, c0/2 and dt (rounded once on the host,
+  // so that FP32 kernels convert nothing per tile)
+  float f_rhoc2, f_inv_rho0, f_half_c0, f_dt;
 };
 
 // The stage kernels' operator result Lv of this thread's node chunk is

@@ -92,85 +92,90 @@ struct Wide {
   static_assert(SN_WORDS >= (size_t)NV * ET * NP, "dt*L of a tile must fit in the face buffer");
 };
 
-// dt*L of the tile in sK ([q][e][i]) -> RK update of the tile in one
-// coalesced float4 pass: the thread's items are taken G at a time, all their
-// operands loaded (u, accumulator and snapshot from global memory, where the
-// tile start prefetched them to L2; u from the stage input in sY in stages 1
-// and 5) before any result is computed and stored.
+// The RK update of a tile in one coalesced float4 pass over its
+// [q][e][i] layout: the thread's items w = tid + k*NT are taken G at a time.
+// wide_rk_load loads the operands of one group (u, accumulator and
+// snapshot from global memory, where the tile start prefetched them to L2;
+// in stages 1 and 5 u from the tile's stage input sY); wide_rk_store
+// combines them with dt*L from sK and writes the results. The first group's
+// loads are issued before the lift, so that their latency overlaps it.
+constexpr int kRkGroup = 3;
+struct RkOps {
+  float4 x0[kRkGroup], x1[kRkGroup], x2[kRkGroup];
+};
+
 template <class C>
-__device__ __forceinline__ void wide_rk_update(const StageArgs<float>& a, const float* sK, const float* sY,
-                                               int64_t e0, int tid, ResAcc<float>& racc) {
+__device__ __forceinline__ void wide_rk_load(const StageArgs<float>& a, const float* sY, int64_t e0, int tid, int k0,
+                                             RkOps& o) {
   constexpr int NP = C::NP, ET = C::ET, NT = C::NT, SEG4 = ET * NP / 4, TILE4 = C::NV * SEG4;
   constexpr int IT = (TILE4 + NT - 1) / NT;  // float4 items of a thread
-  constexpr int G = 3;                       // items whose loads are in flight together
   const int stage = a.stage;
   const bool ld_y = stage == 1 || stage == 5, ld_ua = stage >= 2 && stage <= 4, ld_s = stage == 4;
 #pragma unroll
-  for (int k0 = 0; k0 < IT; k0 += G) {
-    float4 kv[G], x0[G], x1[G], x2[G];
-    int64_t gi[G];
-    int qv[G];
-    bool in[G];
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int w = tid + (k0 + g) * NT;
-      in[g] = tid < NT && k0 + g < IT && w < TILE4;
-      const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
-      const int li = qq * ET * NP + r4 * 4;
-      qv[g] = qq;
-      gi[g] = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
-      kv[g] = x0[g] = x1[g] = x2[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (in[g]) {
-        kv[g] = *reinterpret_cast<const float4*>(sK + li);
-        if (ld_y) x0[g] = *reinterpret_cast<const float4*>(sY + li);
-        if (ld_ua) {
-          x0[g] = __ldcs(reinterpret_cast<const float4*>(a.u + gi[g]));
-          x1[g] = __ldcs(reinterpret_cast<const float4*>(a.acc + gi[g]));
-        }
-        if (ld_s) x2[g] = __ldcs(reinterpret_cast<const float4*>(a.snap + gi[g]));
+  for (int g = 0; g < kRkGroup; ++g) {
+    const int w = tid + (k0 + g) * NT;
+    const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
+    const int64_t gi = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
+    o.x0[g] = o.x1[g] = o.x2[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid < NT && k0 + g < IT && w < TILE4) {
+      if (ld_y) o.x0[g] = *reinterpret_cast<const float4*>(sY + qq * ET * NP + r4 * 4);
+      if (ld_ua) {
+        o.x0[g] = __ldcs(reinterpret_cast<const float4*>(a.u + gi));
+        o.x1[g] = __ldcs(reinterpret_cast<const float4*>(a.acc + gi));
       }
+      if (ld_s) o.x2[g] = __ldcs(reinterpret_cast<const float4*>(a.snap + gi));
     }
+  }
+}
+
+template <class C>
+__device__ __forceinline__ void wide_rk_store(const StageArgs<float>& a, const float* sK, int64_t e0, int tid, int k0,
+                                              const RkOps& o, ResAcc<float>& racc) {
+  constexpr int NP = C::NP, ET = C::ET, NT = C::NT, SEG4 = ET * NP / 4, TILE4 = C::NV * SEG4;
+  constexpr int IT = (TILE4 + NT - 1) / NT;
+  const int stage = a.stage;
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if (!in[g]) continue;
-      const float4 v = kv[g];
-      switch (stage) {
-        case 0:
-          *reinterpret_cast<float4*>(a.k_out + gi[g]) = v;
-          break;
-        case 1: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.acc + gi[g]) = v;
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(y.x + 0.5f * v.x, y.y + 0.5f * v.y, y.z + 0.5f * v.z, y.w + 0.5f * v.w);
-          break;
-        }
-        case 2:
-        case 3: {
-          const float4 u = x0[g], ac = x1[g];
-          const float c = stage == 2 ? 0.5f : 1.0f;
-          *reinterpret_cast<float4*>(a.acc + gi[g]) =
-              make_float4(ac.x + 2.f * v.x, ac.y + 2.f * v.y, ac.z + 2.f * v.z, ac.w + 2.f * v.w);
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(u.x + c * v.x, u.y + c * v.y, u.z + c * v.z, u.w + c * v.w);
-          break;
-        }
-        case 4: {
-          const float4 u = x0[g], ac = x1[g], sn = x2[g];
-          const float4 un = make_float4(u.x + rk4_sixth(ac.x + v.x), u.y + rk4_sixth(ac.y + v.y),
-                                        u.z + rk4_sixth(ac.z + v.z), u.w + rk4_sixth(ac.w + v.w));
-          *reinterpret_cast<float4*>(a.u + gi[g]) = un;
-          racc.add(qv[g], sn.x, un.x, a.c0sq);
-          racc.add(qv[g], sn.y, un.y, a.c0sq);
-          racc.add(qv[g], sn.z, un.z, a.c0sq);
-          racc.add(qv[g], sn.w, un.w, a.c0sq);
-          break;
-        }
-        default: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) = make_float4(y.x + v.x, y.y + v.y, y.z + v.z, y.w + v.w);
-          break;
-        }
+  for (int g = 0; g < kRkGroup; ++g) {
+    const int w = tid + (k0 + g) * NT;
+    if (!(tid < NT && k0 + g < IT && w < TILE4)) continue;
+    const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
+    const int64_t gi = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
+    const float4 v = *reinterpret_cast<const float4*>(sK + qq * ET * NP + r4 * 4);
+    switch (stage) {
+      case 0:
+        *reinterpret_cast<float4*>(a.k_out + gi) = v;
+        break;
+      case 1: {
+        const float4 y = o.x0[g];
+        *reinterpret_cast<float4*>(a.acc + gi) = v;
+        *reinterpret_cast<float4*>(a.y_out + gi) =
+            make_float4(y.x + 0.5f * v.x, y.y + 0.5f * v.y, y.z + 0.5f * v.z, y.w + 0.5f * v.w);
+        break;
+      }
+      case 2:
+      case 3: {
+        const float4 u = o.x0[g], ac = o.x1[g];
+        const float c = stage == 2 ? 0.5f : 1.0f;
+        *reinterpret_cast<float4*>(a.acc + gi) =
+            make_float4(ac.x + 2.f * v.x, ac.y + 2.f * v.y, ac.z + 2.f * v.z, ac.w + 2.f * v.w);
+        *reinterpret_cast<float4*>(a.y_out + gi) = make_float4(u.x + c * v.x, u.y + c * v.y, u.z + c * v.z, u.w + c * v.w);
+        break;
+      }
+      case 4: {
+        const float4 u = o.x0[g], ac = o.x1[g], sn = o.x2[g];
+        const float4 un = make_float4(u.x + rk4_sixth(ac.x + v.x), u.y + rk4_sixth(ac.y + v.y),
+                                      u.z + rk4_sixth(ac.z + v.z), u.w + rk4_sixth(ac.w + v.w));
+        *reinterpret_cast<float4*>(a.u + gi) = un;
+        racc.add(qq, sn.x, un.x, a.c0sq);
+        racc.add(qq, sn.y, un.y, a.c0sq);
+        racc.add(qq, sn.z, un.z, a.c0sq);
+        racc.add(qq, sn.w, un.w, a.c0sq);
+        break;
+      }
+      default: {
+        const float4 y = o.x0[g];
+        *reinterpret_cast<float4*>(a.y_out + gi) = make_float4(y.x + v.x, y.y + v.y, y.z + v.z, y.w + v.w);
+        break;
       }
     }
   }
@@ -186,7 +191,7 @@ __device__ __forceinline__ void wide_tile(const StageArgs<float>& a, int64_t e0,
                                           int nepi, int tid, bool& ok, ResAcc<float>& racc) {
   constexpr int D = C::D, NP = C::NP, NV = C::NV, NK = C::NK, NC = C::NC, NH = C::NH, NSPLIT = C::NSPLIT;
   constexpr int ET = C::ET, RECF = C::RECF, NPR = C::NPR, OVW = C::OVW, NVQ = C::NVQ;
-  const float rhoc2 = (float)a.ph.rhoc2, inv_rho0 = (float)a.ph.inv_rho0, half_c0 = (float)a.ph.half_c0;
+  const float rhoc2 = a.f_rhoc2, inv_rho0 = a.f_inv_rho0, half_c0 = a.f_half_c0;
   // a block larger than this shape's NT (the mixed-order kernel) leaves its
   // other threads idle in this tile; they only take part in the barriers
   const bool active = tid < C::NT;
@@ -304,6 +309,10 @@ __device__ __forceinline__ void wide_tile(const StageArgs<float>& a, int64_t e0,
   if (active) face_fluxes<C, float>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
   __syncthreads();
 
+  // operands of the first group of RK-update items, in flight during the lift
+  RkOps rk;
+  if constexpr (!C::kStaged) wide_rk_load<C>(a, sY, e0, tid, 0, rk);
+
   // ---- lifting (sL holds -LIFT: the products accumulate) ----
   if (active) {
     const float* hrow = sN + (size_t)e * C::SN_EL;
@@ -322,7 +331,7 @@ __device__ __forceinline__ void wide_tile(const StageArgs<float>& a, int64_t e0,
       }
     }
   }
-  const float dte = (float)a.dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
+  const float dte = a.f_dt * sGF[e * RECF + C::S::PHYS_OFF + D];  // dt times the element's step scale
 
   if constexpr (!C::kStaged) {
     // ---- dt*L into the face buffer ([q][e][i]), then the coalesced update ----
@@ -340,7 +349,14 @@ __device__ __forceinline__ void wide_tile(const StageArgs<float>& a, int64_t e0,
         }
     }
     __syncthreads();
-    if (ok) wide_rk_update<C>(a, sK, sY, e0, tid, racc);
+    if (ok) {
+      constexpr int IT = (C::NV * ET * NP / 4 + C::NT - 1) / C::NT;
+#pragma unroll
+      for (int k0 = 0; k0 < IT; k0 += kRkGroup) {
+        if (k0 > 0) wide_rk_load<C>(a, sY, e0, tid, k0, rk);
+        wide_rk_store<C>(a, sK, e0, tid, k0, rk, racc);
+      }
+    }
   } else {
     // ---- RK update from registers ----
     if (nepi > 0 && ok && !mbar_wait(bar_epi, epi_parity, a.wait_limit)) ok = false;
