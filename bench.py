@@ -326,7 +326,7 @@ def run_plain(args, W, rank, world):
                                "note": "3 kind::tf32 products per operand pair (head x head and the two head x tail corrections)"}
     if args.variants:
         per_variant = {}
-        for v in [-1] + list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)) + list(range(48, 64)):
+        for v in [-1] + list(range(8)) + [16, 17, 18, 19, 20, 21, 22] + list(range(32, 40)) + list(range(48, 64)):
             if v >= 0 and S.kernel_info(v)[0] == 0:
                 continue
             S.tune(v)

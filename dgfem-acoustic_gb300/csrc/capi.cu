@@ -275,7 +275,9 @@ cudaError_t launch_stage_t(dg_ctx* c, int stage, const T* y_in, T* y_out, T* k_o
   const dgk::StageArgs<T> a = stage_args<T>(c, stage, y_in, y_out, k_out, dt);
   if (dgk::is_tc_variant(c->variant)) {
     if constexpr (sizeof(T) == 4)
-      return dgk::is_tc2_variant(c->variant)
+      return dgk::is_tc3_variant(c->variant)
+                 ? dgk::launch_stage_tc3(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream)
+             : dgk::is_tc2_variant(c->variant)
                  ? dgk::launch_stage_tc2(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream)
                  : dgk::launch_stage_tc(c->dim, c->order, dgk::tc_npart(c->variant), a, c->grid2, c->d_err, c->stream);
     return cudaErrorInvalidValue;
@@ -483,6 +485,7 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
                                                            : dgk::Stage2Info{0, 0, 0, 0, 0, 0};
   if (dgk::is_tc_variant(v))
     return c->prec != DG_FP32        ? dgk::Stage2Info{0, 0, 0, 0, 0, 0}
+           : dgk::is_tc3_variant(v) ? dgk::stage_tc3_info(c->dim, c->order, dgk::tc_npart(v))
            : dgk::is_tc2_variant(v) ? dgk::stage_tc2_info(c->dim, c->order, dgk::tc_npart(v))
                                     : dgk::stage_tc_info(c->dim, c->order, dgk::tc_npart(v));
   if (c->prec == DG_FP32)
@@ -495,7 +498,7 @@ dgk::Stage2Info stage2_info(const dg_ctx* c, int v) {
 }
 
 // Selects the stage kernel: -1 baseline, k >= 0 pipelined variant k,
-// kTcVariant .. kTcVariant + 4 the tensor-core kernels, kStage3Variant + k
+// kTcVariant .. kTcVariant + 6 the tensor-core kernels, kStage3Variant + k
 // constant-operator variant k, kWideVariant + k flux-form variant k (the
 // last three FP32).
 bool set_variant(dg_ctx* c, int v) {

@@ -203,18 +203,29 @@ Stage2Info stage2_info_f64_1d(int order, int variant);
 // kTcVariant + 1, kTcVariant + 2 of the context's kernel selection are the
 // one-chunk kernel (stage_tc.cuh; 2, 4 or 8 threads per tile row: 256, 512 or
 // 1024 per block), kTcVariant + 3 and kTcVariant + 4 the two-chunk kernel
-// (stage_tc2.cuh, two blocks per SM; 2 or 4 threads per tile row).
+// (stage_tc2.cuh, two blocks per SM; 2 or 4 threads per tile row),
+// kTcVariant + 5 and kTcVariant + 6 the warp-specialised kernel
+// (stage_tc3.cuh; 2 or 4 builder threads per tile row).
 constexpr int kTcVariant = 16;
-constexpr int kTcVariants = 5;
+constexpr int kTcVariants = 7;
 inline bool is_tc_variant(int v) { return v >= kTcVariant && v < kTcVariant + kTcVariants; }
-inline bool is_tc2_variant(int v) { return v >= kTcVariant + 3 && v < kTcVariant + kTcVariants; }
-inline int tc_npart(int v) { return is_tc2_variant(v) ? 2 << (v - kTcVariant - 3) : 2 << (v - kTcVariant); }
+inline bool is_tc2_variant(int v) { return v >= kTcVariant + 3 && v < kTcVariant + 5; }
+inline bool is_tc3_variant(int v) { return v >= kTcVariant + 5 && v < kTcVariant + 7; }
+inline int tc_npart(int v) {
+  return is_tc3_variant(v) ? 2 << (v - kTcVariant - 5) : is_tc2_variant(v) ? 2 << (v - kTcVariant - 3) : 2 << (v - kTcVariant);
+}
 cudaError_t launch_stage_tc(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
                             cudaStream_t s);
 Stage2Info stage_tc_info(int dim, int order, int npart);
 cudaError_t launch_stage_tc2(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
                              cudaStream_t s);
 Stage2Info stage_tc2_info(int dim, int order, int npart);
+// Warp-specialised tensor-core kernel (stage_tc3.cuh, tetrahedra of orders 3
+// and 4, one block per SM): variants kTcVariant + 5 and kTcVariant + 6 (2 or
+// 4 builder threads per tile row).
+cudaError_t launch_stage_tc3(int dim, int order, int npart, const StageArgs<float>& a, int grid, int* err,
+                             cudaStream_t s);
+Stage2Info stage_tc3_info(int dim, int order, int npart);
 // Constant-operator stage kernel (stage3.cuh, FP32 state only): variant ids
 // kStage3Variant + k of the context's kernel selection; the operators are
 // uploaded to constant memory once per device and element type.

@@ -59,7 +59,7 @@ def test_curved_rhs_matches_oracle(pkg, oracle, dim, p, prec, kind):
         if dim == 2:
             assert np.all(k[3] == 0.0)
     # the straight-sided-only kernels are not offered
-    for v in [16, 17, 18, 19, 20, 32]:
+    for v in [16, 17, 18, 19, 20, 21, 22, 32]:
         assert S.kernel_info(v)[0] == 0
         with pytest.raises(pkg.gpu.SolverError):
             S.tune(v)

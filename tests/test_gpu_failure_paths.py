@@ -36,8 +36,9 @@ def _phys(dim):
 
 def _waiting_variants(S):
     """Stage-kernel variants that wait on mbarriers: pipelined (0..7),
-    tensor-core (16-20) and constant-operator (32..) kernels."""
-    return [v for v in list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)) + list(range(48, 64)) if S.kernel_info(v)[0] > 0]
+    tensor-core (16-21), constant-operator (32..) and wide-chunk (48..)
+    kernels."""
+    return [v for v in list(range(8)) + [16, 17, 18, 19, 20, 21, 22] + list(range(32, 40)) + list(range(48, 64)) if S.kernel_info(v)[0] > 0]
 
 
 @pytest.mark.parametrize("dim,p,prec", [(3, 3, "fp32"), (3, 4, "fp32"), (2, 3, "fp32"), (3, 2, "fp64"),

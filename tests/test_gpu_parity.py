@@ -33,7 +33,7 @@ def kernel_variants(pkg, S):
     for S: pipelined (0..), tensor-core (16-20), constant-operator (32..),
     flux-form (48..)."""
     out = [-1]
-    for v in list(range(8)) + [16, 17, 18, 19, 20] + list(range(32, 40)) + list(range(48, 64)):
+    for v in list(range(8)) + [16, 17, 18, 19, 20, 21, 22] + list(range(32, 40)) + list(range(48, 64)):
         if S.kernel_info(v)[0] > 0:
             out.append(v)
     return out
