@@ -23,6 +23,11 @@ namespace dgk {
 // Polling rounds of a bounded device wait (mbarrier try_wait) before it
 // gives up and the kernel reports DG_ERR_TIMEOUT.
 constexpr int kWaitRounds = 1 << 20;
+// Suspend-time hint of each polling round (ns): a waiting thread sleeps until
+// the phase completes or this time has passed, instead of spinning and taking
+// issue slots from the warps that work; a wait ends after at most
+// kWaitRounds x kWaitHintNs (about a second).
+constexpr uint32_t kWaitHintNs = 1000;
 
 constexpr int kCodeLfMask = 0x3;       // neighbour local face
 constexpr int kCodePermShift = 2;      // corner permutation index (3 bits)

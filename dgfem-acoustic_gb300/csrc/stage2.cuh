@@ -64,9 +64,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
   for (int it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(kWaitHintNs)
         : "memory");
     if (ok) return true;
   }
