@@ -30,7 +30,7 @@ NVCCFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-X
                     "-I" + INCLUDE]
 
 HOST_SRC = ["mshio.cpp", "host_mesh.cpp", "host_api.cpp", "refelem.cpp", "config.cpp", "formula.cpp", "outputs.cpp", "quadrature.cpp"]
-GPU_SRC = ["capi.cu", "setup.cu", "stage_f32_2d.cu", "stage_f32_3d.cu", "stage_f64_2d.cu", "stage_f64_3d.cu", "stage_1d.cu", "stage_tc.cu", "stage_tc2.cu", "stage3.cu", "stage4.cu", "stage_multi.cu", "curved.cu", "vtu_writer.cu", "noalloc.cu", "batch.cu", "mlp.cu"]
+GPU_SRC = ["capi.cu", "setup.cu", "stage_f32_2d.cu", "stage_f32_3d.cu", "stage_f64_2d.cu", "stage_f64_3d.cu", "stage_1d.cu", "stage_tc.cu", "stage_tc2.cu", "stage_tc3.cu", "stage3.cu", "stage4.cu", "stage_multi.cu", "curved.cu", "vtu_writer.cu", "noalloc.cu", "batch.cu", "mlp.cu"]
 GPU_HOST_SRC = ["refelem.cpp", "quadrature.cpp"]
 
 

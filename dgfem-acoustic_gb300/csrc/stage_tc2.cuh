@@ -112,8 +112,8 @@ struct Tc2Cfg {
 // TF32 tail at columns COL_AH / col_al + (col - kc0). cf holds the element's
 // coefficients: gv0 (D values), then rho0 c0^2 G (D*D, Q = 0) or G_rQ / rho0
 // (D, Q > 0). The thread takes the 4-node groups j0 = 4*(part + t*NPART);
-// the last group of an NP that is not a multiple of 4 is clamped and padded
-// with zeros.
+// the last group of an NP that is not a multiple of 4 reads the last node
+// again (its columns meet zero rows of B).
 template <class C, int Q>
 __device__ __forceinline__ void tc2_build_vol(const float* sY, const float* cf, int e, int part, uint32_t trow,
                                               int kc0, int kc1, int col_al) {
@@ -159,7 +159,9 @@ __device__ __forceinline__ void tc2_build_vol(const float* sY, const float* cf, 
         } else {
           x = fmaf(cf[D + r], yp[u], cf[r] * yv[0][u]);
         }
-        fr[u] = (j0 + u < NP) ? x : 0.f;
+        // a column past NP (the clamped last node's value, finite) meets
+        // a zero row of B: no mask needed
+        fr[u] = x;
       }
       uint32_t hi[4], lo[4];
       split4(fr, hi, lo);
@@ -231,8 +233,13 @@ __device__ __forceinline__ void tc2_build_face(const float* sN, int q, int e, in
     const int col = KV + c4 * 4;
     if (col < kc0 || col >= kc1) continue;  // warp-uniform
     float x[4];
+    if constexpr (C::KT - KV == NK) {  // no padding columns
 #pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = (c4 * 4 + u < NK) ? hrow[c4 * 4 + u] : 0.f;
+      for (int u = 0; u < 4; ++u) x[u] = hrow[c4 * 4 + u];
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = (c4 * 4 + u < NK) ? hrow[c4 * 4 + u] : 0.f;
+    }
     uint32_t hi[4], lo[4];
     split4(x, hi, lo);
     tmem_st4(trow + C::COL_AH + (col - kc0), hi);

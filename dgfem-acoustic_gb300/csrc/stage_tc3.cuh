@@ -162,7 +162,8 @@ __device__ __forceinline__ void tmem_wait_ld16(uint32_t* r) {
 
 // Volume columns of reference direction r for row (Q, e) into one A region
 // (head at ahi, tail at alo, local column j): the thread takes the 4-node
-// groups j0 = 4 (part + t NPART); nodes past NP give zero columns.
+// groups j0 = 4 (part + t NPART); columns past NP repeat the last node
+// (finite values that meet zero rows of B).
 //   Q = 0 (pressure): gv0_r p_j + sum_d (rho0 c0^2 G_rd) v_d,j
 //   Q = 1+d (v_d):    gv0_r v_d,j + (G_rd / rho0) p_j
 template <class C, int Q>
@@ -197,7 +198,7 @@ __device__ __forceinline__ void tc3_build_vol(const float* sY, const float* cf, 
       } else {
         x = fmaf(cr[1], yp, cr[0] * yq_row[j]);
       }
-      fr[u] = j0 + u < NP ? x : 0.f;
+      fr[u] = x;  // past NP: the last node's value, against a zero row of B
     }
     uint32_t hi[4], lo[4];
     split4(fr, hi, lo);
@@ -229,8 +230,13 @@ __device__ __forceinline__ void tc3_build_face(const float* sN, int q, int e, in
     if (c4 >= NG4) break;
     const int k0 = 4 * c4;
     float x[4];
+    if constexpr (C::KF == NK) {  // no padding columns
 #pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = k0 + u < NK ? hrow[k0 + u] : 0.f;
+      for (int u = 0; u < 4; ++u) x[u] = hrow[k0 + u];
+    } else {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = k0 + u < NK ? hrow[k0 + u] : 0.f;
+    }
     uint32_t hi[4], lo[4];
     split4(x, hi, lo);
     tmem_st4(ahi + k0, hi);
