@@ -597,7 +597,8 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
 
     // ---- epilogue 2: RK update, one coalesced float4 pass over the tile ----
     tc2_rk_update<C>(a, sK, e0, wt, racc);
-    __syncthreads();  // sK (the face buffer) is free for the next tile's gathers
+    // no barrier here: the next tile's first barrier (after its copy wait)
+    // comes before its gathers reuse sK (the face buffer)
   }
 
   // ---- teardown: own copies and tensor-core work first, then the memory ----
