@@ -7,8 +7,9 @@
 namespace dgk {
 
 namespace {
-// per (dim, order): candidate (NC, ET, volume form, operands staged)
-constexpr int F = kFluxForm, W = kWForm;
+// per (dim, order): candidate (NC, ET, volume form, operands staged); form
+// W2 is the W form with two elements per thread
+constexpr int F = kFluxForm, W = kWForm, W2 = kWForm2;
 #define DGK_S4_VARIANTS(X)                                                                            \
   X(2, 1, 4, 128, W, false) X(2, 1, 4, 128, F, true)                                                  \
   X(2, 2, 6, 64, W, false) X(2, 2, 6, 64, F, false) X(2, 2, 6, 64, F, true) X(2, 2, 6, 128, W, false)   \
@@ -17,7 +18,7 @@ constexpr int F = kFluxForm, W = kWForm;
   X(2, 3, 4, 32, W, false) X(2, 3, 10, 64, W, false)                                                  \
   X(2, 4, 8, 32, W, false) X(2, 4, 8, 32, F, false) X(2, 4, 8, 32, F, true) X(2, 4, 8, 64, W, false)    \
   X(2, 4, 4, 32, W, false) X(2, 4, 6, 32, W, false)                                                   \
-  X(3, 3, 2, 32, W, false) X(3, 3, 4, 32, W, false) X(3, 3, 4, 32, F, false)                           \
+  X(3, 3, 2, 32, W, false) X(3, 3, 4, 32, W, false) X(3, 3, 4, 32, F, false) X(3, 3, 2, 32, W2, false)  \
   X(3, 4, 6, 32, W, false) X(3, 4, 4, 32, W, false)
 }  // namespace
 
@@ -43,7 +44,7 @@ Stage2Info stage4_info(int dim, int order, int variant) {
 #define DGK_S4_INFO(DD, PP, CC, EE, FF, SS)                                                   \
   if (dim == DD && order == PP) {                                                            \
     if (k == variant) {                                                                      \
-      using Cf = Wide<DD, PP, CC, EE, FF, SS>;                                               \
+      using Cf = typename Stage4Sel<DD, PP, CC, EE, FF, SS>::C;                              \
       return Stage2Info{Cf::NC, Cf::ET, Cf::NT, (int)Cf::bytes,                              \
                         Stage4<DD, PP, CC, EE, FF, SS>::blocks_per_sm(), n};                 \
     }                                                                                        \

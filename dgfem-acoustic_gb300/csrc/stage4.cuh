@@ -38,7 +38,8 @@
 
 namespace dgk {
 
-constexpr int kFluxForm = 0, kWForm = 1;
+// volume forms: flux form, W form, W form with two elements per thread
+constexpr int kFluxForm = 0, kWForm = 1, kWForm2 = 2;
 
 // Compile-time configuration: element shape (D, P), nodes per thread NC
 // (even), elements per tile ET, the volume form and the operand staging.
@@ -371,6 +372,186 @@ __device__ __forceinline__ void wide_tile(const StageArgs<float>& a, int64_t e0,
   }
 }
 
+// Two elements per thread (W form, operands not staged): a thread owns the
+// same chunk of NC output nodes of elements e and e + ET/2 of the tile, so
+// that every operator entry it loads from shared memory feeds 2 x NV FMAs
+// instead of NV (the volume and lift phases take half the operator
+// wavefronts per element); ET/2 x NSPLIT threads per tile.
+template <int D_, int P, int NC_, int ET_>
+struct WideEB : Wide<D_, P, NC_, ET_, kWForm, false> {
+  using Base = Wide<D_, P, NC_, ET_, kWForm, false>;
+  static constexpr int EB = 2;
+  static constexpr int NT = ET_ / 2 * Base::NSPLIT;
+  static_assert(NT % 32 == 0, "threads per block must be a multiple of 32");
+  static_assert(ET_ % 2 == 0, "two elements per thread");
+};
+
+template <class C>
+__device__ __forceinline__ void wide_mix(const float* sGF, int e, float rhoc2, float inv_rho0,
+                                         const float2 (&W2)[C::D][C::NH][C::NV], float2 (&L2)[C::NH][C::NV]) {
+  constexpr int D = C::D, NH = C::NH, RECF = C::RECF;
+  const float* G = sGF + e * RECF;
+  const float* ev0 = G + C::S::PHYS_OFF;
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float x = G[r * D] * ev0[0];
+#pragma unroll
+    for (int d = 1; d < D; ++d) x = fmaf(G[r * D + d], ev0[d], x);
+    const float2 g0 = make_float2(x, x);
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
+      L2[h][0] = __ffma2_rn(g0, W2[r][h][0], L2[h][0]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const float cpv = rhoc2 * G[r * D + d], cvv = G[r * D + d] * inv_rho0;
+        L2[h][0] = __ffma2_rn(make_float2(cpv, cpv), W2[r][h][1 + d], L2[h][0]);
+        L2[h][1 + d] = __ffma2_rn(g0, W2[r][h][1 + d], L2[h][1 + d]);
+        L2[h][1 + d] = __ffma2_rn(make_float2(cvv, cvv), W2[r][h][0], L2[h][1 + d]);
+      }
+    }
+  }
+}
+
+// One tile of the two-elements-per-thread stage (see WideEB); the arguments
+// are pipe_tile's.
+template <class C>
+__device__ __forceinline__ void wide_eb_tile(const StageArgs<float>& a, int64_t e0, float* sY, const float* sGF,
+                                             const int* sGI, const float* sE, float* sN, const float* sD,
+                                             const float* sL, const short* sFm, const short* sNb, uint64_t* bar_epi,
+                                             uint32_t epi_parity, int nepi, int tid, bool& ok, ResAcc<float>& racc) {
+  constexpr int D = C::D, NP = C::NP, NV = C::NV, NK = C::NK, NC = C::NC, NH = C::NH, NSPLIT = C::NSPLIT;
+  constexpr int ET = C::ET, RECF = C::RECF, NPR = C::NPR, OVW = C::OVW, NVQ = C::NVQ, EH = ET / 2;
+  const float rhoc2 = a.f_rhoc2, inv_rho0 = a.f_inv_rho0, half_c0 = a.f_half_c0;
+  const bool active = tid < C::NT;
+  const int ep = active ? tid / NSPLIT : 0, s = active ? tid - (tid / NSPLIT) * NSPLIT : 0;
+  const int ea = ep, eb = ep + EH;  // the thread's two elements
+  const int i0 = s * NC;
+  // RK operands of this tile towards L2 (read by the coalesced update)
+  if (tid < NV * nepi) {
+    const int k = tid / NV, q = tid - (tid / NV) * NV;
+    const float* src = k == 0 ? a.u : (k == 1 ? a.acc : a.snap);
+    prefetch_l2(src + q * a.stride + e0 * NP, C::YSEG);
+  }
+  // ---- neighbour traces: asynchronous gathers into sN ----
+  if (active) gather_traces<C, float>(a.y_in, a.stride, sGI, sNb, sN, tid, e0);
+  cp_async_commit();
+
+  float2 La[NH][NV], Lb[NH][NV];
+#pragma unroll
+  for (int h = 0; h < NH; ++h)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) La[h][q] = Lb[h][q] = make_float2(0.f, 0.f);
+  if (active) {
+    // ---- volume term per reference direction for both elements, then
+    // the metric mixing per element ----
+    float2 Wa[D][NH][NV], Wb[D][NH][NV];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+      for (int h = 0; h < NH; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) Wa[r][h][q] = Wb[r][h][q] = make_float2(0.f, 0.f);
+    const float* ya = sY + ea * NP;
+    const float* yb = sY + eb * NP;
+#pragma unroll 4
+    for (int j = 0; j < NP; ++j) {
+      float y1[NV], y2[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) y1[q] = ya[q * ET * NP + j], y2[q] = yb[q * ET * NP + j];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float dv[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c += OVW) vload<float, OVW>(dv + c, sD + (r * NP + j) * NPR + i0 + c);
+#pragma unroll
+        for (int h = 0; h < NH; ++h) {
+          const float2 dp = make_float2(dv[2 * h], dv[2 * h + 1]);
+#pragma unroll
+          for (int q = 0; q < NV; ++q) {
+            Wa[r][h][q] = __ffma2_rn(dp, make_float2(y1[q], y1[q]), Wa[r][h][q]);
+            Wb[r][h][q] = __ffma2_rn(dp, make_float2(y2[q], y2[q]), Wb[r][h][q]);
+          }
+        }
+      }
+    }
+    wide_mix<C>(sGF, ea, rhoc2, inv_rho0, Wa, La);
+    wide_mix<C>(sGF, eb, rhoc2, inv_rho0, Wb, Lb);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  // ---- face numerical fluxes (in place of the gathered traces) ----
+  if (active) face_fluxes<C, float>(a.bmat, sY, sGF, sGI, sFm, sNb, sN, tid, rhoc2, inv_rho0, half_c0, e0);
+  __syncthreads();
+
+  // operands of the first group of RK-update items, in flight during the lift
+  RkOps rk;
+  wide_rk_load<C>(a, sY, e0, tid, 0, rk);
+
+  // ---- lifting for both elements (sL holds -LIFT) ----
+  if (active) {
+    const float* ha = sN + (size_t)ea * C::SN_EL;
+    const float* hb = sN + (size_t)eb * C::SN_EL;
+#pragma unroll 4
+    for (int k = 0; k < NK; ++k) {
+      float h1[NVQ], h2[NVQ];
+      vload<float, NVQ>(h1, ha + k * NVQ);
+      vload<float, NVQ>(h2, hb + k * NVQ);
+      float lv[NC];
+#pragma unroll
+      for (int c = 0; c < NC; c += OVW) vload<float, OVW>(lv + c, sL + k * NPR + i0 + c);
+#pragma unroll
+      for (int h = 0; h < NH; ++h) {
+        const float2 lp = make_float2(lv[2 * h], lv[2 * h + 1]);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          La[h][q] = __ffma2_rn(lp, make_float2(h1[q], h1[q]), La[h][q]);
+          Lb[h][q] = __ffma2_rn(lp, make_float2(h2[q], h2[q]), Lb[h][q]);
+        }
+      }
+    }
+  }
+  // ---- dt*L into the face buffer ([q][e][i]), then the coalesced update ----
+  const float dta = a.f_dt * sGF[ea * RECF + C::S::PHYS_OFF + D];
+  const float dtb = a.f_dt * sGF[eb * RECF + C::S::PHYS_OFF + D];
+  float* sK = sN;
+  __syncthreads();  // every thread has read the face fluxes
+  if (active) {
+#pragma unroll
+    for (int h = 0; h < NH; ++h)
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int i = i0 + 2 * h + u;
+        if (i < NP)
+#pragma unroll
+          for (int q = 0; q < NV; ++q) {
+            sK[(q * ET + ea) * NP + i] = dta * (u ? La[h][q].y : La[h][q].x);
+            sK[(q * ET + eb) * NP + i] = dtb * (u ? Lb[h][q].y : Lb[h][q].x);
+          }
+      }
+  }
+  __syncthreads();
+  if (ok) {
+    constexpr int IT = (C::NV * ET * NP / 4 + C::NT - 1) / C::NT;
+#pragma unroll
+    for (int k0 = 0; k0 < IT; k0 += kRkGroup) {
+      if (k0 > 0) wide_rk_load<C>(a, sY, e0, tid, k0, rk);
+      wide_rk_store<C>(a, sK, e0, tid, k0, rk, racc);
+    }
+  }
+}
+
+struct WideEBTileOps {
+  template <class C, typename T>
+  __device__ static void load_ops(T* sD, T* sL, const StageArgs<T>& a, int tid, int nthreads = C::NT);
+  template <class C, typename T>
+  __device__ static void run(const StageArgs<T>& a, int64_t e0, T* sY, const T* sGF, const int* sGI, const T* sE,
+                             T* sN, const T* sD, const T* sL, const short* sFm, const short* sNb, uint64_t* bar_epi,
+                             uint32_t epi_parity, int nepi, int tid, bool& ok, ResAcc<T>& racc) {
+    wide_eb_tile<C>(a, e0, sY, sGF, sGI, sE, sN, sD, sL, sFm, sNb, bar_epi, epi_parity, nepi, tid, ok, racc);
+  }
+};
+
 // Operator tables (zero-padded rows) and tile body of the wide-chunk kernel.
 struct WideTileOps {
   template <class C, typename T>
@@ -393,16 +574,35 @@ struct WideTileOps {
   }
 };
 
+template <class C, typename T>
+__device__ void WideEBTileOps::load_ops(T* sD, T* sL, const StageArgs<T>& a, int tid, int nthreads) {
+  WideTileOps::load_ops<C, T>(sD, sL, a, tid, nthreads);
+}
+
+// configuration and tile body of a variant (FORM kWForm2: two elements per
+// thread, operands not staged)
 template <int D, int P, int NC_, int ET_, int FORM, bool STAGED>
-__global__ void __launch_bounds__(Wide<D, P, NC_, ET_, FORM, STAGED>::NT)
+struct Stage4Sel {
+  using C = Wide<D, P, NC_, ET_, FORM, STAGED>;
+  using Ops = WideTileOps;
+};
+template <int D, int P, int NC_, int ET_, bool STAGED>
+struct Stage4Sel<D, P, NC_, ET_, kWForm2, STAGED> {
+  using C = WideEB<D, P, NC_, ET_>;
+  using Ops = WideEBTileOps;
+};
+
+template <int D, int P, int NC_, int ET_, int FORM, bool STAGED>
+__global__ void __launch_bounds__(Stage4Sel<D, P, NC_, ET_, FORM, STAGED>::C::NT)
     stage4_kernel(const StageArgs<float> a, int* err) {
   extern __shared__ __align__(128) unsigned char sm[];
-  pipe_loop<Wide<D, P, NC_, ET_, FORM, STAGED>, float, WideTileOps>(a, err, sm);
+  using Sel = Stage4Sel<D, P, NC_, ET_, FORM, STAGED>;
+  pipe_loop<typename Sel::C, float, typename Sel::Ops>(a, err, sm);
 }
 
 template <int D, int P, int NC_, int ET_, int FORM, bool STAGED>
 struct Stage4 {
-  using C = Wide<D, P, NC_, ET_, FORM, STAGED>;
+  using C = typename Stage4Sel<D, P, NC_, ET_, FORM, STAGED>::C;
   static cudaError_t set_attrs() {
     auto kfn = stage4_kernel<D, P, NC_, ET_, FORM, STAGED>;
     cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::bytes);
