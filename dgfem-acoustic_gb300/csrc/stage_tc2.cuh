@@ -48,6 +48,16 @@ struct Tc2Cfg {
   static constexpr int NPART = NPART_;     // threads per row: columns split NPART ways
   static constexpr int NT = 128 * NPART;   // lane quarters x parts
   static constexpr int RECF = S::RECF, RECI = S::RECI;
+  // RK update: the first kRkEarly float4 items of a thread have their
+  // operands loaded before the last MMA chunk's wait (0: none); the
+  // accumulator columns are read in kEpiPasses passes (registers)
+  static constexpr int kRkEarly = 2;
+  static constexpr int kEpiPasses = 2;
+  // neighbour gathers issued after the barrier that publishes the
+  // per-element values, in the same phase as the first chunk's volume
+  // columns (the pressure rows' warps, with more volume columns, take fewer
+  // gather items), rather than before it
+  static constexpr bool kGatherWithVolume = true;
   // face buffer: one plane per variable [NV][ET][NKP] (gather_traces /
   // face_fluxes strides); it also holds dt*L of the tile [NV][ET][NP] in the
   // epilogue
@@ -256,114 +266,139 @@ __device__ __forceinline__ void tc2_build_face(const float* sN, int q, int e, in
 // products (D still small), the second chunk to its own accumulator DC,
 // which the epilogue adds to D. (The operator is split exactly, split_op22;
 // the dropped A_lo B_lo is below 2^-22 of a product.)
-template <class C>
-__device__ __forceinline__ void tc2_mma_chunk(uint32_t tbase, uint32_t bh, uint32_t bl, uint32_t idesc, int kc0,
-                                              int kc1, int col_al, int dcorr, bool first, uint64_t* bar) {
-#pragma unroll 1
+//
+// The whole issuing warp runs this in converged control flow and only its
+// lane 0 executes the MMAs (single-thread instructions): every operand is a
+// compile-time offset from warp-uniform bases (B descriptors: the start
+// address field advanced by the K step's byte offset / 16; operand
+// addresses stay below 256 KB, so the 14-bit field does not carry), and the
+// loops unroll into a straight run of MMAs. (Issued from one divergent
+// thread with descriptors built per MMA, a 39-MMA chunk took about 100
+// cycles per MMA, several times the tensor core's time for it.)
+template <class C, int KC0, int KC1, int COL_AL_, int DCORR, bool FIRST>
+__device__ __forceinline__ void tc2_mma_chunk(uint32_t tbase, uint64_t dbh, uint64_t dbl, uint32_t idesc,
+                                              bool lane0, uint64_t* bar) {
+#pragma unroll
   for (int pass = 0; pass < 3; ++pass) {
-    const uint32_t acol = pass == 0 ? col_al : C::COL_AH;
-    const uint32_t bsrc = pass == 1 ? bl : bh;
-    const uint32_t dcol = pass < 2 ? dcorr : C::COL_D;
+    const uint32_t acol = pass == 0 ? COL_AL_ : C::COL_AH;
+    const uint64_t db = pass == 1 ? dbl : dbh;
+    const uint32_t dcol = pass < 2 ? DCORR : C::COL_D;
     // the first MMA into an accumulator that starts empty overwrites it
-    const bool init0 = (pass == 0 && (first || dcorr != C::COL_D));
-#pragma unroll 1
-    for (int ks = 0; ks < (kc1 - kc0) / 8; ++ks)
-      umma_tf32_ts(tbase + dcol, tbase + acol + ks * 8, umma_desc(bsrc + (kc0 / 8 + ks) * 2 * C::LBO, C::LBO, C::SBO),
-                   idesc, (init0 && ks == 0) ? 0u : 1u);
+    const bool init0 = pass == 0 && (FIRST || DCORR != C::COL_D);
+#pragma unroll
+    for (int ks = 0; ks < (KC1 - KC0) / 8; ++ks) {
+      const uint64_t off = (uint64_t)(((KC0 / 8 + ks) * 2 * C::LBO) >> 4);
+      if (lane0) umma_tf32_ts(tbase + dcol, tbase + acol + ks * 8, db + off, idesc, (init0 && ks == 0) ? 0u : 1u);
+    }
   }
-  umma_commit(bar);
+  if (lane0) umma_commit(bar);
+  __syncwarp();
 }
 
-// The RK update of a tile (elements e0 ..) from dt*L in sK: the thread's
-// float4 items are taken G at a time, the operands of all G (u, accumulator,
-// snapshot or stage input from global memory, prefetched to L2 when the
-// tile started) loaded before any update is computed and stored, so that
-// their loads are in flight together.
-template <class C>
-__device__ __forceinline__ void tc2_rk_update(const StageArgs<float>& a, const float* sK, int64_t e0, int wt,
-                                              ResAcc<float>& racc) {
-  constexpr int NP = C::NP, ET = C::ET, NT = C::NT, SEG4 = ET * NP / 4;
+// The RK update of a tile (elements e0 ..) from dt*L in sK, one coalesced
+// float4 pass: the thread's items are taken G at a time, the operands of all
+// G (u, accumulator, snapshot or stage input from global memory, prefetched
+// to L2 when the tile started) loaded before any update is computed and
+// stored, so that their loads are in flight together. The first group's
+// loads are issued early (tc2_rk_load before the last MMA chunk's wait), so
+// that their latency overlaps that wait.
+template <class C, int G_>
+struct Tc2RkGroup {
+  static constexpr int G = G_;  // items whose loads are in flight together
+  float4 x0[G], x1[G], x2[G];
+  int64_t gi[G];  // offset in the state arrays
+  int so[G];      // offset in sK
+  int qv[G];      // variable
+  bool in[G];
+};
+
+template <class C, int G>
+__device__ __forceinline__ void tc2_rk_load(const StageArgs<float>& a, int64_t e0, int wt, int k0,
+                                            Tc2RkGroup<C, G>& r) {
+  constexpr int NP = C::NP, NT = C::NT, SEG4 = C::ET * NP / 4;
   constexpr int IT = (C::TILE4 + NT - 1) / NT;  // float4 items of the thread
-  constexpr int G = C::NPART == 2 ? 3 : 2;       // items whose loads are in flight together
   const int stage = a.stage;
   const bool ld_y = stage == 1 || stage == 5, ld_ua = stage >= 2 && stage <= 4, ld_s = stage == 4;
-#pragma unroll 1
-  for (int k0 = 0; k0 < IT; k0 += G) {
-    float4 kv[G], x0[G], x1[G], x2[G];
-    int64_t gi[G];
-    int qv[G];
-    bool in[G];
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int w = wt + (k0 + g) * NT;
-      in[g] = k0 + g < IT && w < C::TILE4;
-      const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
-      qv[g] = qq;
-      gi[g] = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
-      kv[g] = x0[g] = x1[g] = x2[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (in[g]) {
-        kv[g] = *reinterpret_cast<const float4*>(sK + (size_t)qq * ET * NP + r4 * 4);
-        if (ld_y) x0[g] = *reinterpret_cast<const float4*>(a.y_in + gi[g]);
-        if (ld_ua) {
-          x0[g] = *reinterpret_cast<const float4*>(a.u + gi[g]);
-          x1[g] = *reinterpret_cast<const float4*>(a.acc + gi[g]);
-        }
-        if (ld_s) x2[g] = *reinterpret_cast<const float4*>(a.snap + gi[g]);
+  for (int g = 0; g < G; ++g) {
+    const int w = wt + (k0 + g) * NT;
+    r.in[g] = k0 + g < IT && w < C::TILE4;
+    const int qq = w / SEG4, r4 = w - (w / SEG4) * SEG4;
+    r.qv[g] = qq;
+    r.so[g] = qq * C::ET * NP + r4 * 4;
+    r.gi[g] = qq * a.stride + e0 * NP + (int64_t)r4 * 4;
+    r.x0[g] = r.x1[g] = r.x2[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r.in[g]) {
+      if (ld_y) r.x0[g] = *reinterpret_cast<const float4*>(a.y_in + r.gi[g]);
+      if (ld_ua) {
+        r.x0[g] = *reinterpret_cast<const float4*>(a.u + r.gi[g]);
+        r.x1[g] = *reinterpret_cast<const float4*>(a.acc + r.gi[g]);
       }
+      if (ld_s) r.x2[g] = *reinterpret_cast<const float4*>(a.snap + r.gi[g]);
     }
+  }
+}
+
+template <class C, int G>
+__device__ __forceinline__ void tc2_rk_finish(const StageArgs<float>& a, const float* sK, const Tc2RkGroup<C, G>& r,
+                                              ResAcc<float>& racc) {
+  const int stage = a.stage;
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if (!in[g]) continue;
-      const float4 v = kv[g];
-      switch (stage) {
-        case 0:
-          *reinterpret_cast<float4*>(a.k_out + gi[g]) = v;
-          break;
-        case 1: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.acc + gi[g]) = v;
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(y.x + 0.5f * v.x, y.y + 0.5f * v.y, y.z + 0.5f * v.z, y.w + 0.5f * v.w);
-          break;
-        }
-        case 2:
-        case 3: {
-          const float4 u = x0[g], ac = x1[g];
-          const float c = stage == 2 ? 0.5f : 1.0f;
-          *reinterpret_cast<float4*>(a.acc + gi[g]) =
-              make_float4(ac.x + 2.f * v.x, ac.y + 2.f * v.y, ac.z + 2.f * v.z, ac.w + 2.f * v.w);
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) =
-              make_float4(u.x + c * v.x, u.y + c * v.y, u.z + c * v.z, u.w + c * v.w);
-          break;
-        }
-        case 4: {
-          const float4 u = x0[g], ac = x1[g], sn = x2[g];
-          const float4 un = make_float4(u.x + rk4_sixth(ac.x + v.x), u.y + rk4_sixth(ac.y + v.y),
-                                        u.z + rk4_sixth(ac.z + v.z), u.w + rk4_sixth(ac.w + v.w));
-          *reinterpret_cast<float4*>(a.u + gi[g]) = un;
-          racc.add(qv[g], sn.x, un.x, a.c0sq);
-          racc.add(qv[g], sn.y, un.y, a.c0sq);
-          racc.add(qv[g], sn.z, un.z, a.c0sq);
-          racc.add(qv[g], sn.w, un.w, a.c0sq);
-          break;
-        }
-        default: {
-          const float4 y = x0[g];
-          *reinterpret_cast<float4*>(a.y_out + gi[g]) = make_float4(y.x + v.x, y.y + v.y, y.z + v.z, y.w + v.w);
-          break;
-        }
+  for (int g = 0; g < G; ++g) {
+    if (!r.in[g]) continue;
+    const float4 v = *reinterpret_cast<const float4*>(sK + r.so[g]);
+    switch (stage) {
+      case 0:
+        *reinterpret_cast<float4*>(a.k_out + r.gi[g]) = v;
+        break;
+      case 1: {
+        const float4 y = r.x0[g];
+        *reinterpret_cast<float4*>(a.acc + r.gi[g]) = v;
+        *reinterpret_cast<float4*>(a.y_out + r.gi[g]) =
+            make_float4(y.x + 0.5f * v.x, y.y + 0.5f * v.y, y.z + 0.5f * v.z, y.w + 0.5f * v.w);
+        break;
+      }
+      case 2:
+      case 3: {
+        const float4 u = r.x0[g], ac = r.x1[g];
+        const float c = stage == 2 ? 0.5f : 1.0f;
+        *reinterpret_cast<float4*>(a.acc + r.gi[g]) =
+            make_float4(ac.x + 2.f * v.x, ac.y + 2.f * v.y, ac.z + 2.f * v.z, ac.w + 2.f * v.w);
+        *reinterpret_cast<float4*>(a.y_out + r.gi[g]) =
+            make_float4(u.x + c * v.x, u.y + c * v.y, u.z + c * v.z, u.w + c * v.w);
+        break;
+      }
+      case 4: {
+        const float4 u = r.x0[g], ac = r.x1[g], sn = r.x2[g];
+        const float4 un = make_float4(u.x + rk4_sixth(ac.x + v.x), u.y + rk4_sixth(ac.y + v.y),
+                                      u.z + rk4_sixth(ac.z + v.z), u.w + rk4_sixth(ac.w + v.w));
+        *reinterpret_cast<float4*>(a.u + r.gi[g]) = un;
+        racc.add(r.qv[g], sn.x, un.x, a.c0sq);
+        racc.add(r.qv[g], sn.y, un.y, a.c0sq);
+        racc.add(r.qv[g], sn.z, un.z, a.c0sq);
+        racc.add(r.qv[g], sn.w, un.w, a.c0sq);
+        break;
+      }
+      default: {
+        const float4 y = r.x0[g];
+        *reinterpret_cast<float4*>(a.y_out + r.gi[g]) = make_float4(y.x + v.x, y.y + v.y, y.z + v.z, y.w + v.w);
+        break;
       }
     }
   }
 }
 
 template <int D, int P, int NPART>
-__global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
+__global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, 2)
     stage_tc2_kernel(const StageArgs<float> a, int* err) {
   using C = Tc2Cfg<D, P, NPART>;
   constexpr int NP = C::NP, NF = C::NF, NFP = C::NFP, NV = C::NV, NPERM = C::NPERM, NK = C::NK;
   constexpr int ET = C::ET, NT = C::NT, RECF = C::RECF, KV = C::KV, KT = C::KT, KC = C::KC, NCH = C::NCH;
   constexpr int NN = C::NN, GT = C::GT;
+  // float4 items of the RK update per thread, and those loaded early
+  constexpr bool EARLY = C::kRkEarly > 0;
+  constexpr int RK_IT = (C::TILE4 + NT - 1) / NT, RK_G0 = RK_IT < 3 ? RK_IT : 3;
+  constexpr int RK_E = EARLY ? (RK_IT < C::kRkEarly ? RK_IT : C::kRkEarly) : RK_G0;
   extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::oBar);  // 0: tile copy, 1: MMA chunks
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + C::oBar + 64);
@@ -463,7 +498,9 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
   uint32_t mma_phase = 0;  // MMA commits waited for so far (bar[1] parity)
   if (leader && (int)blockIdx.x < a.ntiles) issue_tile(blockIdx.x), arm(0, 0);
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-  const uint32_t bh = smem_u32(sBh), bl = smem_u32(sBl);
+  const uint64_t dbh = umma_desc(smem_u32(sBh), C::LBO, C::SBO), dbl = umma_desc(smem_u32(sBl), C::LBO, C::SBO);
+  // the MMA warp (the leader's), as a warp-uniform value
+  const bool mma_warp = __shfl_sync(0xffffffffu, warp, 0) == NT / 32 - 1;
   static_assert(NCH == 1 || KV >= KC, "face columns must lie in the last K chunk");
 
   // Each mbarrier is polled by the leader alone; the block learns the outcome
@@ -488,8 +525,10 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
       prefetch_l2(src + qq * stride + e0 * NP, C::YSEG);
     }
     // ---- neighbour traces (asynchronous) ----
-    gather_traces<C, float>(a.y_in, stride, sGI, sNb, sN, wt, e0);
-    cp_async_commit();
+    if constexpr (!C::kGatherWithVolume) {
+      gather_traces<C, float>(a.y_in, stride, sGI, sNb, sN, wt, e0);
+      cp_async_commit();
+    }
     // ---- per-element values of the row phase, element-minor ----
     for (int w = wt; w < ET * GT; w += NT) {
       const int el = w / GT, v = w - (w / GT) * GT;
@@ -497,6 +536,10 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
       sGT[v * (ET + 1) + el] = sGF[el * RECF + src];
     }
     __syncthreads();
+    if constexpr (C::kGatherWithVolume) {
+      gather_traces<C, float>(a.y_in, stride, sGI, sNb, sN, wt, e0);
+      cp_async_commit();
+    }
     float cf[D + D * D];
     if (row_ok) {
       tc2_coeffs<C>(sGT, q, e, rhoc2, inv_rho0, cf);
@@ -511,7 +554,8 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
     __syncthreads();
     tc_fence_after();
     if constexpr (NCH == 2) {
-      if (leader) tc2_mma_chunk<C>(tbase, bh, bl, idesc, 0, KC, C::COL_AL, C::COL_D, true, &bar[1]), arm(1, mma_phase);
+      if (mma_warp) tc2_mma_chunk<C, 0, KC, C::COL_AL, C::COL_D, true>(tbase, dbh, dbl, idesc, leader, &bar[1]);
+      if (leader) arm(1, mma_phase);
     }
     // ---- face numerical fluxes (in place of the gathered traces; they
     // overlap the first chunk's MMAs) ----
@@ -534,16 +578,21 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
       __syncthreads();  // the face fluxes are in sN
     }
     if (row_ok) tc2_build_face<C>(sN, q, e, part, trow, NCH == 2 ? KC : 0, KT, NCH == 2 ? C::COL_AL2 : C::COL_AL);
+    // the first RK-operand loads, in flight through the last chunk's MMAs
+    Tc2RkGroup<C, RK_E> rk0;
+    if constexpr (EARLY) tc2_rk_load<C>(a, e0, wt, 0, rk0);
     tmem_wait_st();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     bool gm2 = true;
-    if (leader) {
+    if (mma_warp) {
       if constexpr (NCH == 2)
-        tc2_mma_chunk<C>(tbase, bh, bl, idesc, KC, KT, C::COL_AL2, C::COL_DC, false, &bar[1]);
+        tc2_mma_chunk<C, KC, KT, C::COL_AL2, C::COL_DC, false>(tbase, dbh, dbl, idesc, leader, &bar[1]);
       else
-        tc2_mma_chunk<C>(tbase, bh, bl, idesc, 0, KT, C::COL_AL, C::COL_D, true, &bar[1]);
+        tc2_mma_chunk<C, 0, KT, C::COL_AL, C::COL_D, true>(tbase, dbh, dbl, idesc, leader, &bar[1]);
+    }
+    if (leader) {
       arm(1, mma_phase);
       // the tile buffer has been consumed: the next tile's copies overlap
       // this chunk's MMAs and the epilogue
@@ -560,43 +609,55 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, NPART == 4 ? 2 : 1)
     }
     tc_fence_after();
 
-    // ---- epilogue 1: dt*L of this thread's row into sK ([q][e][i]) ----
+    // ---- epilogue 1: dt*L of this thread's row into sK ([q][e][i]), the
+    // accumulator columns in kEpiPasses passes ----
     if (row_ok) {
       const float dte = dt * sGT[(D * D + D) * (ET + 1) + e];
       float* kr = sK + (size_t)(q * ET + e) * NP;
-      constexpr int NCHK = (NN / 4 + NPART - 1) / NPART;
-      uint32_t dr[NCHK][4], dc[NCHK][4];
+      constexpr int NCHK = (NN / 4 + NPART - 1) / NPART, NPASS = C::kEpiPasses;
+      constexpr int NHALF = (NCHK + NPASS - 1) / NPASS;
 #pragma unroll
-      for (int t = 0; t < NCHK; ++t) {
-        const int c4 = part + t * NPART;
-        if (c4 * 4 < NP) {  // warp-uniform condition
-          tmem_ld4_async(trow + C::COL_D + c4 * 4, dr[t]);
-          if constexpr (NCH == 2) tmem_ld4_async(trow + C::COL_DC + c4 * 4, dc[t]);
-        }
-      }
+      for (int h = 0; h < NPASS; ++h) {
+        uint32_t dr[NHALF][4], dc[NHALF][4];
 #pragma unroll
-      for (int t = 0; t < NCHK; ++t)
-        if ((part + t * NPART) * 4 < NP) {
-          tmem_wait_ld4(dr[t]);
-          if constexpr (NCH == 2) tmem_wait_ld4(dc[t]);
+        for (int tt = 0; tt < NHALF; ++tt) {
+          const int c4 = part + (h * NHALF + tt) * NPART;
+          if (h * NHALF + tt < NCHK && c4 * 4 < NP) {  // warp-uniform condition
+            tmem_ld4_async(trow + C::COL_D + c4 * 4, dr[tt]);
+            if constexpr (NCH == 2) tmem_ld4_async(trow + C::COL_DC + c4 * 4, dc[tt]);
+          }
         }
 #pragma unroll
-      for (int t = 0; t < NCHK; ++t) {
-        const int i0 = (part + t * NPART) * 4;
-        if (i0 >= NP) break;  // warp-uniform
+        for (int tt = 0; tt < NHALF; ++tt)
+          if (h * NHALF + tt < NCHK && (part + (h * NHALF + tt) * NPART) * 4 < NP) {
+            tmem_wait_ld4(dr[tt]);
+            if constexpr (NCH == 2) tmem_wait_ld4(dc[tt]);
+          }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          float x = __uint_as_float(dr[t][u]);
-          if constexpr (NCH == 2) x += __uint_as_float(dc[t][u]);
-          if (i0 + u < NP) kr[i0 + u] = dte * x;
+        for (int tt = 0; tt < NHALF; ++tt) {
+          const int i0 = (part + (h * NHALF + tt) * NPART) * 4;
+          if (h * NHALF + tt >= NCHK || i0 >= NP) break;  // warp-uniform
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float x = __uint_as_float(dr[tt][u]);
+            if constexpr (NCH == 2) x += __uint_as_float(dc[tt][u]);
+            if (i0 + u < NP) kr[i0 + u] = dte * x;
+          }
         }
       }
     }
     tc_fence_before();
     __syncthreads();
 
-    // ---- epilogue 2: RK update, one coalesced float4 pass over the tile ----
-    tc2_rk_update<C>(a, sK, e0, wt, racc);
+    // ---- epilogue 2: RK update, one coalesced float4 pass over the tile:
+    // the early group, then the thread's other items in one group ----
+    if constexpr (!EARLY) tc2_rk_load<C>(a, e0, wt, 0, rk0);
+    tc2_rk_finish<C>(a, sK, rk0, racc);
+    if constexpr (RK_IT > RK_E) {
+      Tc2RkGroup<C, RK_IT - RK_E> rk1;
+      tc2_rk_load<C>(a, e0, wt, RK_E, rk1);
+      tc2_rk_finish<C>(a, sK, rk1, racc);
+    }
     // no barrier here: the next tile's first barrier (after its copy wait)
     // comes before its gathers reuse sK (the face buffer)
   }
