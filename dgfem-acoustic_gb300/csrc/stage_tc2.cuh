@@ -53,6 +53,10 @@ struct Tc2Cfg {
   // accumulator columns are read in kEpiPasses passes (registers)
   static constexpr int kRkEarly = 2;
   static constexpr int kEpiPasses = 2;
+  // A's tail (x - TF32(x)) handed to the MMA as FP32 bits: the tensor core
+  // reads its TF32 bits, which drops the second rounding instruction per A
+  // value (tail error at most 2^-21 of the value instead of 2^-22)
+  static constexpr bool kRawTail = true;
   // neighbour gathers issued after the barrier that publishes the
   // per-element values, in the same phase as the first chunk's volume
   // columns (the pressure rows' warps, with more volume columns, take fewer
@@ -112,6 +116,20 @@ struct Tc2Cfg {
   static_assert(YSEG % 16 == 0, "tile segments must be 16-byte multiples");
   static_assert(bytes <= 227 * 1024, "shared memory of one block exceeds 227 KB");
 };
+
+// Head and tail of 4 A values (split4, or with the tail as FP32 bits: kRawTail)
+template <class C>
+__device__ __forceinline__ void tc2_split4(const float* x, uint32_t* hi, uint32_t* lo) {
+  if constexpr (C::kRawTail) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      hi[u] = tf32_rna(x[u]);
+      lo[u] = __float_as_uint(x[u] - __uint_as_float(hi[u]));
+    }
+  } else {
+    split4(x, hi, lo);
+  }
+}
 
 // Volume columns [kc0, kc1) of row (Q, e) into tensor memory, the variable
 // Q fixed at compile time (each warp owns rows of one variable):
@@ -174,7 +192,7 @@ __device__ __forceinline__ void tc2_build_vol(const float* sY, const float* cf, 
         fr[u] = x;
       }
       uint32_t hi[4], lo[4];
-      split4(fr, hi, lo);
+      tc2_split4<C>(fr, hi, lo);
       tmem_st4(trow + C::COL_AH + (col - kc0), hi);
       tmem_st4(trow + col_al + (col - kc0), lo);
     }
@@ -251,7 +269,7 @@ __device__ __forceinline__ void tc2_build_face(const float* sN, int q, int e, in
       for (int u = 0; u < 4; ++u) x[u] = (c4 * 4 + u < NK) ? hrow[c4 * 4 + u] : 0.f;
     }
     uint32_t hi[4], lo[4];
-    split4(x, hi, lo);
+    tc2_split4<C>(x, hi, lo);
     tmem_st4(trow + C::COL_AH + (col - kc0), hi);
     tmem_st4(trow + col_al + (col - kc0), lo);
   }
@@ -541,6 +559,7 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, 2)
       cp_async_commit();
     }
     float cf[D + D * D];
+    Tc2RkGroup<C, RK_E> rk0;  // the first RK-update operands
     if (row_ok) {
       tc2_coeffs<C>(sGT, q, e, rhoc2, inv_rho0, cf);
       // ---- volume columns of the first chunk ----
@@ -579,7 +598,6 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, 2)
     }
     if (row_ok) tc2_build_face<C>(sN, q, e, part, trow, NCH == 2 ? KC : 0, KT, NCH == 2 ? C::COL_AL2 : C::COL_AL);
     // the first RK-operand loads, in flight through the last chunk's MMAs
-    Tc2RkGroup<C, RK_E> rk0;
     if constexpr (EARLY) tc2_rk_load<C>(a, e0, wt, 0, rk0);
     tmem_wait_st();
     tc_fence_before();
