@@ -231,25 +231,27 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
     const T* ye = sY + el * NP;
     T* srow = sN + (size_t)el * C::SN_EL + f * NFP * C::SN_K;
     const short* fm = sFm + f * NFP;
+    // h holds the flux already scaled by sJ (the per-face coefficients
+    // below carry the scale)
     auto put = [&](int m, const T (&h)[NV]) {
       T* slot = srow + m * C::SN_K;
       if constexpr (C::SN_Q == 1) {
         T hv[C::NVQ];
 #pragma unroll
-        for (int q = 0; q < C::NVQ; ++q) hv[q] = q < NV ? sJ * h[q < NV ? q : 0] : (T)0;
+        for (int q = 0; q < C::NVQ; ++q) hv[q] = q < NV ? h[q < NV ? q : 0] : (T)0;
         vstore<T, C::NVQ>(slot, hv);
       } else {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) slot[(size_t)q * C::SN_Q] = sJ * h[q];
+        for (int q = 0; q < NV; ++q) slot[(size_t)q * C::SN_Q] = h[q];
       }
     };
     if (code & kCodeBoundary) {
-      T B[NV][NV];
+      T B[NV][NV];  // sJ * the boundary matrix
       const T* Bg = bmat + (int64_t)nbr * NV * NV;
 #pragma unroll
       for (int q = 0; q < NV; ++q)
 #pragma unroll
-        for (int qq = 0; qq < NV; ++qq) B[q][qq] = __ldg(Bg + q * NV + qq);
+        for (int qq = 0; qq < NV; ++qq) B[q][qq] = sJ * __ldg(Bg + q * NV + qq);
 #pragma unroll
       for (int mm = 0; mm < FS::MC; ++mm) {
         const int m = mm * FS::FCH + ch;
@@ -276,6 +278,13 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
       T vn0 = ev0[0] * n[0];
 #pragma unroll
       for (int d = 1; d < D; ++d) vn0 += ev0[d] * n[d];
+      // sJ h = (sJ vn0 / 2) avg + (sJ n / 2) (rho0 c0^2 avg_v, avg_p / rho0)
+      //        + (sJ hc) dif
+      const T hsJ = (T)0.5 * sJ;
+      const T a0 = hsJ * vn0, hcs = sJ * hc;
+      T np_[3], nu_[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) np_[d] = hsJ * rhoc2 * n[d], nu_[d] = hsJ * inv_rho0 * n[d];
 #pragma unroll
       for (int mm = 0; mm < FS::MC; ++mm) {
         const int m = mm * FS::FCH + ch;
@@ -302,12 +311,12 @@ __device__ __forceinline__ void face_fluxes(const T* __restrict__ bmat, const T*
         T avg[NV], dif[NV];
 #pragma unroll
         for (int q = 0; q < NV; ++q) avg[q] = um[q] + up[q], dif[q] = um[q] - up[q];
-        T nv = n[0] * avg[1];
+        T x = a0 * avg[0];
 #pragma unroll
-        for (int d = 1; d < D; ++d) nv += n[d] * avg[1 + d];
-        h[0] = (T)0.5 * (vn0 * avg[0] + rhoc2 * nv) + hc * dif[0];
+        for (int d = 0; d < D; ++d) x += np_[d] * avg[1 + d];
+        h[0] = x + hcs * dif[0];
 #pragma unroll
-        for (int d = 0; d < D; ++d) h[1 + d] = (T)0.5 * (vn0 * avg[1 + d] + n[d] * avg[0] * inv_rho0) + hc * dif[1 + d];
+        for (int d = 0; d < D; ++d) h[1 + d] = a0 * avg[1 + d] + nu_[d] * avg[0] + hcs * dif[1 + d];
         put(m, h);
       }
     }
