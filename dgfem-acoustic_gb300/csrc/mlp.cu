@@ -9,11 +9,18 @@
 // (FP32 master copies for the optimiser), activations and gradients in FP32,
 // every sum accumulated in FP32.
 //
-// Kernels: one tiled GEMM (64 x 64 output tile, 16-deep K slices staged in
-// shared memory, 4 x 4 outputs per thread) serves the three products of a
-// layer: Z = X W^T (forward), dX = dZ W (input gradient) and dW = dZ^T X
-// (weight gradient); element-wise GELU and its derivative, the MSE gradient,
-// bias reductions and an Adam step complete the training loop.
+// Kernels: one GEMM serves the three products of a layer: Z = X W^T
+// (forward), dX = dZ W (input gradient) and dW = dZ^T X (weight gradient),
+// on the CUDA cores (k_gemm: 64 x 64 output tile, 16-deep K slices staged in
+// shared memory, 4 x 4 outputs per thread; the default) or on the tensor
+// cores (k_gemm_tc, tcgen05 kind::tf32; dg_mlp_set_tensor_cores). At this
+// network's sizes (layers of at most 512, 256-2000 rows) the CUDA-core GEMM
+// is the faster: the tensor-core one stages and splits each K slice and waits
+// for its MMAs before the next (GB300, the 6-256-256-256-256-512 network:
+// forward of 2000 rows 0.31 against 0.63 ms, a training step of 256 rows
+// 0.68 against 0.87 ms, host arrays);
+// element-wise GELU and its derivative, the MSE gradient, bias reductions
+// and an Adam step complete the training loop.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -26,6 +33,7 @@
 #include <vector>
 
 #include "../../include/dgfem_gb300.h"
+#include "stage_tc.cuh"  // tcgen05, mbarrier and shared-memory descriptor helpers
 
 namespace dgc {
 void set_global_error(const std::string& m);
@@ -98,6 +106,161 @@ __global__ void __launch_bounds__(GT) k_gemm(int M, int N, int K, const TA* __re
       }
     }
   }
+}
+
+// Tensor-core GEMM (sm_103a tcgen05, kind::tf32), same contract as k_gemm:
+// C[m][n] = sum_k A(m,k) B(k,n) (+ bias[n]) over a 128 x 64 output tile per
+// block of 128 threads, K in slices of 32. Each slice is staged in shared
+// memory in the canonical K-major no-swizzle layout (8-row x 16-byte core
+// matrices): A (FP32 activations or gradients) as a TF32 head and tail, B
+// the same when it is FP32 (activations, in the weight gradient) and as it
+// is when it holds BF16 weights (exact in TF32). One thread issues the
+// slice's MMAs, A_lo B_hi (+ A_hi B_lo) + A_hi B_hi, accumulating in FP32 in
+// 64 tensor-memory columns, and commits to an mbarrier that the block waits
+// for (bounded) before the next slice overwrites the operands; the epilogue
+// reads the accumulator rows (tcgen05.ld, one lane quarter per warp) and
+// applies k_gemm's epilogue. A block whose wait gives up sets *err, waits
+// (default limit) for its MMAs in flight and frees its tensor memory.
+constexpr int TBM = 128, TBN = 64, TBK = 32, TGT = 128;
+constexpr uint32_t T_LBO_A = (TBM / 8) * 128, T_LBO_B = (TBN / 8) * 128;  // K-adjacent core matrices
+constexpr uint32_t T_ABYTES = TBM * TBK * 4, T_BBYTES = TBN * TBK * 4;
+constexpr size_t T_SMEM = 2 * (size_t)T_ABYTES + 2 * (size_t)T_BBYTES + 32;  // + mbarrier, tensor-memory slot
+
+// byte offset of (row, k) in a [rows][TBK] operand slice (core matrices of
+// 8 rows x 4 values, row groups adjacent, then K groups)
+__device__ __forceinline__ uint32_t tc_off(int row, int k, int rows) {
+  return (uint32_t)(((k >> 2) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::tf32, FP32 accumulate.
+__device__ __forceinline__ void umma_tf32_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                             uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+template <typename TB>
+__global__ void __launch_bounds__(TGT) k_gemm_tc(int M, int N, int K, const float* __restrict__ A, int64_t sam,
+                                                 int64_t sak, const TB* __restrict__ B, int64_t sbk, int64_t sbn,
+                                                 const float* __restrict__ bias, float* __restrict__ Z,
+                                                 float* __restrict__ Y, int ldc, int mode, int* __restrict__ err) {
+  constexpr bool BSPLIT = sizeof(TB) == 4;
+  extern __shared__ __align__(128) unsigned char smt[];
+  unsigned char* sAh = smt;
+  unsigned char* sAl = sAh + T_ABYTES;
+  unsigned char* sBh = sAl + T_ABYTES;
+  unsigned char* sBl = sBh + T_BBYTES;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sBl + T_BBYTES);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sBl + T_BBYTES + 16);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
+  if (tid == 0) {
+    dgk::mbar_init(bar, 1);
+    dgk::fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dgk::smem_u32(tslot)),
+                 "r"((uint32_t)TBN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  dgk::tc_fence_before();
+  __syncthreads();
+  dgk::tc_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t idesc =
+      (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TBN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+  const uint64_t dah = dgk::umma_desc(dgk::smem_u32(sAh), T_LBO_A, 128);
+  const uint64_t dal = dgk::umma_desc(dgk::smem_u32(sAl), T_LBO_A, 128);
+  const uint64_t dbh = dgk::umma_desc(dgk::smem_u32(sBh), T_LBO_B, 128);
+  const uint64_t dbl = dgk::umma_desc(dgk::smem_u32(sBl), T_LBO_B, 128);
+  bool ok = true, pend = false;  // pend: a commit not yet observed complete (thread 0)
+  uint32_t phase = 0;
+  for (int k0 = 0; k0 < K; k0 += TBK) {
+    // ---- the slice's operands, zero outside the matrices ----
+    for (int i = tid; i < TBM * TBK; i += TGT) {
+      const int mm = i / TBK, kk = i - (i / TBK) * TBK, m = m0 + mm, k = k0 + kk;
+      const float x = (m < M && k < K) ? A[(int64_t)m * sam + (int64_t)k * sak] : 0.f;
+      const uint32_t h = dgk::tf32_rna(x), off = tc_off(mm, kk, TBM);
+      *reinterpret_cast<uint32_t*>(sAh + off) = h;
+      *reinterpret_cast<uint32_t*>(sAl + off) = dgk::tf32_rna(x - __uint_as_float(h));
+    }
+    for (int i = tid; i < TBN * TBK; i += TGT) {
+      const int nn = i / TBK, kk = i - (i / TBK) * TBK, n = n0 + nn, k = k0 + kk;
+      const float x = (n < N && k < K) ? ldf(B + (int64_t)k * sbk + (int64_t)n * sbn) : 0.f;
+      const uint32_t off = tc_off(nn, kk, TBN);
+      if constexpr (BSPLIT) {
+        const uint32_t h = dgk::tf32_rna(x);
+        *reinterpret_cast<uint32_t*>(sBh + off) = h;
+        *reinterpret_cast<uint32_t*>(sBl + off) = dgk::tf32_rna(x - __uint_as_float(h));
+      } else {
+        *reinterpret_cast<uint32_t*>(sBh + off) = __float_as_uint(x);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // read by the tensor cores
+    dgk::tc_fence_before();
+    __syncthreads();
+    dgk::tc_fence_after();
+    bool got = true;
+    if (tid == 0) {
+#pragma unroll
+      for (int ks = 0; ks < TBK / 8; ++ks) {
+        const uint64_t oa = (uint64_t)((ks * 2 * T_LBO_A) >> 4), ob = (uint64_t)((ks * 2 * T_LBO_B) >> 4);
+        umma_tf32_ss(tbase, dal + oa, dbh + ob, idesc, (k0 == 0 && ks == 0) ? 0u : 1u);
+        if constexpr (BSPLIT) umma_tf32_ss(tbase, dah + oa, dbl + ob, idesc, 1u);
+        umma_tf32_ss(tbase, dah + oa, dbh + ob, idesc, 1u);
+      }
+      dgk::umma_commit(bar);
+      got = dgk::mbar_wait(bar, phase & 1u);
+      pend = !got;
+    }
+    ++phase;
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    dgk::tc_fence_after();
+  }
+  if (ok) {
+    // ---- epilogue: row m0 + 32 warp + lane, TBN columns ----
+    const int m = m0 + warp * 32 + lane;
+    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < TBN; c0 += 16) {
+      uint32_t r[4][4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) dgk::tmem_ld4_async(trow + c0 + 4 * t, r[t]);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) dgk::tmem_wait_ld4(r[t]);
+      if (m >= M) continue;
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int n = n0 + c0 + 4 * t + u;
+          if (n >= N) continue;
+          const float c = __uint_as_float(r[t][u]) + (bias ? bias[n] : 0.f);
+          if (mode == 0) {
+            Z[(int64_t)m * ldc + n] = c;
+            Y[(int64_t)m * ldc + n] = 0.5f * c * (1.f + erff(c * 0.70710678118654752f));
+          } else {
+            Y[(int64_t)m * ldc + n] = c;
+          }
+        }
+    }
+  }
+  // ---- teardown: the MMAs in flight after a give-up, then the memory ----
+  if (tid == 0 && pend) dgk::mbar_wait(bar, (phase - 1) & 1u);
+  if (tid == 0 && !ok) atomicOr(err, 1);
+  dgk::tc_fence_before();
+  __syncthreads();
+  dgk::tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"((uint32_t)TBN)
+                 : "memory");
 }
 
 // dZ = dY * GELU'(Z), GELU'(z) = Phi(z) + z phi(z)
@@ -199,6 +362,8 @@ struct dg_mlp {
   int* bidx = nullptr;
   int64_t n_data = 0, bcap = 0;
   int64_t step = 0;  // Adam steps taken
+  int tc = 0;             // GEMMs on the tensor cores (k_gemm_tc), else k_gemm
+  int* d_err = nullptr;   // set by a tensor-core GEMM whose wait gave up
   std::string err;
 };
 
@@ -240,6 +405,39 @@ int ensure_cap(dg_mlp* m, int64_t n) {
   return DG_OK;
 }
 
+// One GEMM of a layer (k_gemm's contract) on the tensor cores or the CUDA
+// cores, on the network's stream.
+template <typename TB>
+int gemm(dg_mlp* m, int M, int N, int K, const float* A, int64_t sam, int64_t sak, const TB* B, int64_t sbk,
+         int64_t sbn, const float* bias, float* Z, float* Y, int ldc, int mode) {
+  if (m->tc) {
+    static bool configured = false;
+    if (!configured) {
+      MCK(m, cudaFuncSetAttribute(k_gemm_tc<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T_SMEM));
+      configured = true;
+    }
+    dim3 grid(nblk(N, TBN), nblk(M, TBM));
+    k_gemm_tc<TB><<<grid, TGT, T_SMEM, m->stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, Z, Y, ldc, mode, m->d_err);
+  } else {
+    dim3 grid(nblk(N, BN), nblk(M, BM));
+    k_gemm<float, TB><<<grid, GT, 0, m->stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, Z, Y, ldc, mode);
+  }
+  MCK(m, cudaGetLastError());
+  return DG_OK;
+}
+
+// After a stream synchronisation: DG_ERR_TIMEOUT (and the flag cleared) when
+// a tensor-core GEMM gave up waiting for its MMAs.
+int check_gemm_waits(dg_mlp* m) {
+  int h = 0;
+  MCK(m, cudaMemcpyAsync(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  MCK(m, cudaStreamSynchronize(m->stream));
+  if (h == 0) return DG_OK;
+  MCK(m, cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream));
+  MCK(m, cudaStreamSynchronize(m->stream));
+  return fail(m, DG_ERR_TIMEOUT, "dg_mlp: a tensor-core GEMM timed out waiting for its MMAs");
+}
+
 int refresh_bf16(dg_mlp* m) {
   const int L = (int)m->w.size() - 1;
   for (int l = 0; l < L; ++l) {
@@ -255,13 +453,11 @@ int forward(dg_mlp* m, int64_t n) {
   const int L = (int)m->w.size() - 1;
   for (int l = 0; l < L; ++l) {
     const int K = m->w[l], N = m->w[l + 1];
-    dim3 grid(nblk(N, BN), nblk(n, BM));
     const bool last = l == L - 1;
-    k_gemm<float, __nv_bfloat16><<<grid, GT, 0, m->stream>>>((int)n, N, K, m->X[l], K, 1, m->wh + m->hoff[l], 1, K,
-                                                             m->p + m->boff[l], m->Z[l + 1], m->X[l + 1], N,
-                                                             last ? 1 : 0);
+    const int rc = gemm<__nv_bfloat16>(m, (int)n, N, K, m->X[l], K, 1, m->wh + m->hoff[l], 1, K, m->p + m->boff[l],
+                                       m->Z[l + 1], m->X[l + 1], N, last ? 1 : 0);
+    if (rc != DG_OK) return rc;
   }
-  MCK(m, cudaGetLastError());
   return DG_OK;
 }
 
@@ -280,15 +476,13 @@ int backward(dg_mlp* m, int64_t n) {
       std::swap(dcur, dnext);  // dcur now holds dZ
     }
     // dW[N][K] = dZ^T X: rows n of W, columns k, summed over the batch
-    dim3 gw(nblk(K, BN), nblk(N, BM));
-    k_gemm<float, float><<<gw, GT, 0, m->stream>>>(N, K, (int)n, dZ, 1, N, m->X[l], K, 1, nullptr, nullptr,
-                                                   m->g + m->woff[l], K, 1);
+    int rc = gemm<float>(m, N, K, (int)n, dZ, 1, N, m->X[l], K, 1, nullptr, nullptr, m->g + m->woff[l], K, 1);
+    if (rc != DG_OK) return rc;
     k_colsum<<<nblk(N, 128), 128, 0, m->stream>>>(dZ, (int)n, N, m->g + m->boff[l]);
     if (l > 0) {
       // dX[n][K] = dZ W
-      dim3 gx(nblk(K, BN), nblk(n, BM));
-      k_gemm<float, __nv_bfloat16><<<gx, GT, 0, m->stream>>>((int)n, K, N, dZ, N, 1, m->wh + m->hoff[l], K, 1,
-                                                             nullptr, nullptr, dnext, K, 1);
+      rc = gemm<__nv_bfloat16>(m, (int)n, K, N, dZ, N, 1, m->wh + m->hoff[l], K, 1, nullptr, nullptr, dnext, K, 1);
+      if (rc != DG_OK) return rc;
       std::swap(dcur, dnext);
     }
   }
@@ -334,6 +528,8 @@ int dg_mlp_create(int n_layers, const int* widths, int device, dg_mlp** out) {
   if (e == cudaSuccess) e = cudaMalloc(&m->wh, m->n_wts * sizeof(__nv_bfloat16));
   if (e == cudaSuccess) e = cudaMalloc(&m->part, 64 * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&m->loss, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->d_err, 0, sizeof(int), m->stream);
   // on the network's own (non-blocking) stream: a legacy-stream memset would
   // not be ordered with the uploads that follow
   for (float* q : {m->p, m->g, m->m1, m->m2})
@@ -355,7 +551,7 @@ int dg_mlp_destroy(dg_mlp* m) {
   for (float* q : m->Z) cudaFree(q);
   for (void* q : {(void*)m->p, (void*)m->g, (void*)m->m1, (void*)m->m2, (void*)m->wh, (void*)m->dA, (void*)m->dB,
                   (void*)m->part, (void*)m->loss, (void*)m->tx, (void*)m->ty, (void*)m->bx, (void*)m->by,
-                  (void*)m->bidx})
+                  (void*)m->bidx, (void*)m->d_err})
     cudaFree(q);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
@@ -416,7 +612,7 @@ int dg_mlp_forward(dg_mlp* m, const float* x, int64_t n, float* y) {
   if (rc != DG_OK) return rc;
   MCK(m, cudaMemcpyAsync(y, m->X[L], n * m->w[L] * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
   MCK(m, cudaStreamSynchronize(m->stream));
-  return DG_OK;
+  return check_gemm_waits(m);
 }
 
 int dg_mlp_gradient(dg_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss) {
@@ -440,6 +636,7 @@ int dg_mlp_gradient(dg_mlp* m, const float* x, const float* t, int64_t n, float*
   }
   cudaFree(dt);
   if (e != cudaSuccess) return fail(m, DG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  if (rc == DG_OK) rc = check_gemm_waits(m);
   return rc;
 }
 
@@ -516,7 +713,16 @@ int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_fin
   cudaFree(m->bidx);
   m->bidx = nullptr;
   if (e != cudaSuccess) return fail(m, DG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  if (rc == DG_OK) rc = check_gemm_waits(m);
   return rc;
 }
+
+int dg_mlp_set_tensor_cores(dg_mlp* m, int on) {
+  if (!m) return fail(m, DG_ERR_ARG, "dg_mlp_set_tensor_cores: invalid argument");
+  m->tc = on ? 1 : 0;
+  return DG_OK;
+}
+
+int dg_mlp_tensor_cores(const dg_mlp* m) { return m && m->tc ? 1 : 0; }
 
 }  // extern "C"

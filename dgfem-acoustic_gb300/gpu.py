@@ -26,7 +26,7 @@ SYMBOLS = ["dg_create", "dg_destroy", "dg_last_error", "dg_get_info", "dg_set_st
            "dg_batch_fused",
            "dg_mlp_create", "dg_mlp_destroy", "dg_mlp_last_error", "dg_mlp_param_count", "dg_mlp_set_params",
            "dg_mlp_get_params", "dg_mlp_forward", "dg_mlp_forward_device", "dg_mlp_gradient", "dg_mlp_set_data",
-           "dg_mlp_train"]
+           "dg_mlp_train", "dg_mlp_set_tensor_cores", "dg_mlp_tensor_cores"]
 
 
 class MeshDesc(C.Structure):
@@ -494,6 +494,8 @@ def _mlp_lib():
     L.dg_mlp_gradient.argtypes = [C.c_void_p, P(F), P(F), I64, P(F), P(D)]
     L.dg_mlp_set_data.argtypes = [C.c_void_p, P(F), P(F), I64]
     L.dg_mlp_train.argtypes = [C.c_void_p, I64, C.c_int, D, D, D, C.c_uint64, P(D)]
+    L.dg_mlp_set_tensor_cores.argtypes = [C.c_void_p, C.c_int]
+    L.dg_mlp_tensor_cores.argtypes = [C.c_void_p]
     L._mlp = True
     return L
 
@@ -567,6 +569,14 @@ class Network:
         self._x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.widths[0])
         self._t = np.ascontiguousarray(t, dtype=np.float32).reshape(self._x.shape[0], self.widths[-1])
         self._ck(_mlp_lib().dg_mlp_set_data(self.h, _fp(self._x), _fp(self._t), self._x.shape[0]), "dg_mlp_set_data")
+
+    def set_tensor_cores(self, on):
+        """GEMMs on the tensor cores or on the CUDA cores (the default)."""
+        self._ck(_mlp_lib().dg_mlp_set_tensor_cores(self.h, 1 if on else 0), "dg_mlp_set_tensor_cores")
+
+    @property
+    def tensor_cores(self):
+        return bool(_mlp_lib().dg_mlp_tensor_cores(self.h))
 
     def train(self, n_steps, batch, lr, lr_final, seed=0, weight_decay=0.0):
         losses = np.zeros(max(n_steps, 1))

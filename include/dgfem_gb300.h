@@ -315,6 +315,13 @@ int dg_mlp_set_data(dg_mlp* m, const float* x, const float* t, int64_t n);
  * cosine; losses (optional) receives each step's batch loss */
 int dg_mlp_train(dg_mlp* m, int64_t n_steps, int batch, double lr, double lr_final, double weight_decay, uint64_t seed,
                  double* losses);
+/* The layers' GEMMs on the tensor cores (on != 0: tcgen05 kind::tf32,
+ * activations and gradients as TF32 head + tail, BF16 weights exact in TF32,
+ * FP32 accumulation; a wait for the MMAs that runs out makes the synchronous
+ * calls return DG_ERR_TIMEOUT) or on the CUDA cores (0, the default, faster
+ * at the surrogate's sizes). */
+int dg_mlp_set_tensor_cores(dg_mlp* m, int on);
+int dg_mlp_tensor_cores(const dg_mlp* m);
 
 #ifdef __cplusplus
 }

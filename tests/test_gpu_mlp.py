@@ -1,5 +1,6 @@
 """The surrogate network's GPU kernels (dg_mlp_*) against the CPU oracle
-(oracle/mlp_ref.py): forward pass, loss and parameter gradient, and a short
+(oracle/mlp_ref.py): forward pass, loss and parameter gradient with the
+GEMMs on the tensor cores and on the CUDA cores (the default), and a short
 training run. The GPU accumulates in FP32 with BF16 weights; the oracle uses
 the same BF16 weights in float64."""
 import os
@@ -18,13 +19,18 @@ pytestmark = pytest.mark.gpu
 SURROGATE_WIDTHS = [6, 256, 256, 256, 256, 512]
 
 
-@pytest.mark.parametrize("widths,n", [([6, 32, 32, 7], 5), ([6, 256, 256, 256, 256, 512], 300)])
-def test_forward_matches_oracle(pkg, widths, n):
+@pytest.mark.parametrize("tc", [True, False])
+@pytest.mark.parametrize("widths,n", [([6, 32, 32, 7], 5), ([6, 256, 256, 256, 256, 512], 300),
+                                      ([6, 100, 70, 9], 131)])
+def test_forward_matches_oracle(pkg, widths, n, tc):
     rng = np.random.default_rng(1)
     p = mlp_ref.init_params(widths, seed=2)
     p[mlp_ref.n_params(widths) - widths[-1]:] = rng.normal(0, 0.1, widths[-1])
     x = rng.normal(size=(n, widths[0])).astype(np.float32)
     net = pkg.gpu.Network(widths)
+    assert not net.tensor_cores
+    net.set_tensor_cores(tc)
+    assert net.tensor_cores == tc
     net.set_params(p)
     np.testing.assert_array_equal(net.get_params(), p)
     y = net.forward(x)
@@ -32,13 +38,15 @@ def test_forward_matches_oracle(pkg, widths, n):
     assert rel_l2(y, y_ref) <= 1e-5
 
 
-@pytest.mark.parametrize("widths,n", [([6, 32, 32, 7], 9), (SURROGATE_WIDTHS, 128)])
-def test_gradient_matches_oracle(pkg, widths, n):
+@pytest.mark.parametrize("tc", [True, False])
+@pytest.mark.parametrize("widths,n", [([6, 32, 32, 7], 9), (SURROGATE_WIDTHS, 128), ([6, 100, 70, 9], 200)])
+def test_gradient_matches_oracle(pkg, widths, n, tc):
     rng = np.random.default_rng(4)
     p = mlp_ref.init_params(widths, seed=5)
     x = rng.normal(size=(n, widths[0])).astype(np.float32)
     t = rng.normal(size=(n, widths[-1])).astype(np.float32)
     net = pkg.gpu.Network(widths)
+    net.set_tensor_cores(tc)
     net.set_params(p)
     g, loss = net.gradient(x, t)
     loss_ref, g_ref = mlp_ref.loss_and_grad(p, widths, x, t)
