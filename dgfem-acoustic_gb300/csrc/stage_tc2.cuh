@@ -23,8 +23,13 @@
 //   * the RK operands are not staged: the epilogue writes dt*L of the tile
 //     into shared memory in the state's [q][e][i] layout, then one coalesced
 //     float4 pass over the tile reads u, the accumulator and the snapshot
-//     from global memory (prefetched to L2 when the tile starts) and writes
-//     the new values straight back.
+//     from global memory (prefetched to L2 when the tile starts; a thread's
+//     first items loaded before the last chunk's wait) and writes the new
+//     values straight back;
+//   * the MMAs are issued by one converged warp as an unrolled run (one lane
+//     executes them), the neighbour gathers share the phase of the first
+//     chunk's volume columns, and A's tails go to the MMAs unrounded (the
+//     schedule was set by timing each phase of a tile on the SM clock).
 // 3-D p = 4: 109 KB of shared memory and 256 tensor-memory columns per block.
 // Every wait is bounded (StageArgs::wait_limit polling rounds); a block that
 // gives up issues no further copy or MMA, waits (default limit) for its own
