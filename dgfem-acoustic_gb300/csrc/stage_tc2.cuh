@@ -57,6 +57,9 @@ struct Tc2Cfg {
   // operands loaded before the last MMA chunk's wait (0: none); the
   // accumulator columns are read in kEpiPasses passes (registers)
   static constexpr int kRkEarly = 2;
+  // the other items' operand loads issued before the epilogue's barrier
+  // (after the accumulator columns are read, whose registers are free then)
+  static constexpr bool kRkRestEarly = true;
   static constexpr int kEpiPasses = 2;
   // A's tail (x - TF32(x)) handed to the MMA as FP32 bits: the tensor core
   // reads its TF32 bits, which drops the second rounding instruction per A
@@ -669,6 +672,9 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, 2)
         }
       }
     }
+    constexpr int RK_N1 = RK_IT > RK_E ? RK_IT - RK_E : 1;
+    Tc2RkGroup<C, RK_N1> rk1;  // the thread's other items
+    if constexpr (RK_IT > RK_E && C::kRkRestEarly) tc2_rk_load<C>(a, e0, wt, RK_E, rk1);
     tc_fence_before();
     __syncthreads();
 
@@ -677,8 +683,7 @@ __global__ void __launch_bounds__(Tc2Cfg<D, P, NPART>::NT, 2)
     if constexpr (!EARLY) tc2_rk_load<C>(a, e0, wt, 0, rk0);
     tc2_rk_finish<C>(a, sK, rk0, racc);
     if constexpr (RK_IT > RK_E) {
-      Tc2RkGroup<C, RK_IT - RK_E> rk1;
-      tc2_rk_load<C>(a, e0, wt, RK_E, rk1);
+      if constexpr (!C::kRkRestEarly) tc2_rk_load<C>(a, e0, wt, RK_E, rk1);
       tc2_rk_finish<C>(a, sK, rk1, racc);
     }
     // no barrier here: the next tile's first barrier (after its copy wait)
